@@ -1,0 +1,195 @@
+"""ctypes binding of libgtd.so (the C ABI declared in include/gtd.h).
+
+The library is built in-tree by gisbdw_gb300/build.py. There is no CPU
+fallback: if the library is missing or cannot load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from typing import Optional, Tuple
+
+import numpy as np
+
+from . import build as _build
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u64 = ctypes.c_uint64
+
+STATUS = {
+    0: "GTD_OK", 1: "GTD_INVALID_ARG", 2: "GTD_NOT_CONNECTED", 3: "GTD_OOM",
+    4: "GTD_TIMEOUT", 5: "GTD_ABORTED", 6: "GTD_CUDA_ERROR", 7: "GTD_NO_RESULT",
+}
+DP_MAX_N = 36
+
+
+class GtdError(RuntimeError):
+    """A gtd call returned a status other than GTD_OK."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.status_name = STATUS.get(status, f"status {status}")
+        super().__init__(f"{self.status_name}: {message}")
+
+
+class InvalidArgument(GtdError, ValueError):
+    """GTD_INVALID_ARG / GTD_NOT_CONNECTED (the reference throws
+    std::invalid_argument: elimination_tree.hpp:171-179)."""
+
+
+class DeadlineExceeded(GtdError, TimeoutError):
+    """GTD_TIMEOUT."""
+
+
+def _error(status: int, message: str) -> GtdError:
+    if status in (1, 2):
+        return InvalidArgument(status, message)
+    if status == 4:
+        return DeadlineExceeded(status, message)
+    return GtdError(status, message)
+
+
+class DpOpts(ctypes.Structure):
+    _fields_ = [("tile_bits", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("timeout_ns", ctypes.c_uint64)]
+
+
+class DpStats(ctypes.Structure):
+    _fields_ = [("dp_ms", ctypes.c_float), ("tree_ms", ctypes.c_float),
+                ("total_ms", ctypes.c_float), ("table_bytes", ctypes.c_uint64),
+                ("alg_bytes", ctypes.c_uint64), ("tile_bits", ctypes.c_int),
+                ("tiles", ctypes.c_int), ("ctas", ctypes.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_LIB = None
+_LOCK = threading.Lock()
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads libgtd.so, building it first when it is missing or stale."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        if build_if_missing and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError(f"gtd native library not found at {_build.LIB}; run gisbdw_gb300.build.build()")
+        L = ctypes.CDLL(_build.LIB)
+        L.gtd_create.argtypes = [ctypes.POINTER(_vp), _i, _vp]
+        L.gtd_destroy.argtypes = [_vp]
+        L.gtd_status_string.restype = ctypes.c_char_p
+        L.gtd_status_string.argtypes = [_i]
+        L.gtd_last_error.restype = ctypes.c_char_p
+        L.gtd_last_error.argtypes = [_vp]
+        L.gtd_dp_solve.argtypes = [_vp, _vp, _i, _vp, _vp, _vp, ctypes.POINTER(DpOpts), ctypes.POINTER(DpStats)]
+        L.gtd_dp_solve_device.argtypes = [_vp, _vp, _i, _vp, _vp, _vp, ctypes.POINTER(DpOpts)]
+        L.gtd_sync.argtypes = [_vp, ctypes.POINTER(DpStats)]
+        L.gtd_dp_query.argtypes = [_vp, _u64, _vp, _vp]
+        L.gtd_dp_table.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_u64),
+                                   ctypes.POINTER(_i), ctypes.POINTER(_i)]
+        L.gtd_dp_table_index.restype = _u64
+        L.gtd_dp_table_index.argtypes = [_i, _i, _u64]
+        if hasattr(L, "gtd_dp_read_table"):
+            L.gtd_dp_read_table.argtypes = [_vp, _vp, _u64]
+        _LIB = L
+        return L
+
+
+def _ptr(a: np.ndarray) -> ctypes.c_void_p:
+    return a.ctypes.data_as(_vp)
+
+
+class Handle:
+    """One gtd handle: a CUDA device, a stream and the device buffers."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        self.L = load()
+        self._h = _vp()
+        st = self.L.gtd_create(ctypes.byref(self._h), device, _vp(stream) if stream else None)
+        if st != 0:
+            raise _error(st, f"gtd_create(device={device}) failed")
+
+    def _check(self, st: int) -> None:
+        if st != 0:
+            raise _error(st, self.L.gtd_last_error(self._h).decode())
+
+    def close(self) -> None:
+        if self._h:
+            self.L.gtd_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- subset DP --------------------------------------------------------
+    def dp_solve(self, adj: np.ndarray, n: int, tile_bits: int = 0, ctas_per_sm: int = 0,
+                 timeout_ns: int = 0, want_order: bool = True):
+        """Returns (td, parent[n], order[n] or None, stats dict)."""
+        adj = np.ascontiguousarray(adj, dtype=np.uint64)
+        if adj.size < n:
+            raise ValueError("adjacency shorter than n")
+        td = ctypes.c_int32()
+        parent = np.zeros(n, dtype=np.int32)
+        order = np.zeros(n, dtype=np.int32) if want_order else None
+        opts = DpOpts(tile_bits, ctas_per_sm, timeout_ns)
+        stats = DpStats()
+        self._check(self.L.gtd_dp_solve(self._h, _ptr(adj), n, ctypes.byref(td), _ptr(parent),
+                                        _ptr(order) if want_order else None, ctypes.byref(opts),
+                                        ctypes.byref(stats)))
+        return td.value, parent, order, stats.as_dict()
+
+    def dp_solve_device(self, d_adj: int, n: int, d_td: int, d_parent: int, d_order: int = 0,
+                        tile_bits: int = 0, ctas_per_sm: int = 0, timeout_ns: int = 0) -> None:
+        opts = DpOpts(tile_bits, ctas_per_sm, timeout_ns)
+        self._check(self.L.gtd_dp_solve_device(self._h, _vp(d_adj), n, _vp(d_td), _vp(d_parent),
+                                               _vp(d_order) if d_order else None, ctypes.byref(opts)))
+
+    def sync(self) -> dict:
+        stats = DpStats()
+        self._check(self.L.gtd_sync(self._h, ctypes.byref(stats)))
+        return stats.as_dict()
+
+    def dp_query(self, subset_mask: int, want_order: bool = True):
+        td = ctypes.c_int32()
+        k = bin(subset_mask).count("1")
+        order = np.zeros(max(k, 1), dtype=np.int32)
+        self._check(self.L.gtd_dp_query(self._h, subset_mask, ctypes.byref(td),
+                                        _ptr(order) if want_order else None))
+        return td.value, (order[:k].tolist() if want_order else None)
+
+    def dp_table_info(self) -> Tuple[int, int, int, int]:
+        ptr, nbytes, n, lb = _vp(), _u64(), _i(), _i()
+        self._check(self.L.gtd_dp_table(self._h, ctypes.byref(ptr), ctypes.byref(nbytes),
+                                        ctypes.byref(n), ctypes.byref(lb)))
+        return ptr.value or 0, nbytes.value, n.value, lb.value
+
+    def dp_read_table(self) -> Tuple[np.ndarray, int, int]:
+        """Raw table bytes (tiled layout), n and tile bits of the last solve."""
+        _, nbytes, n, lb = self.dp_table_info()
+        out = np.empty(nbytes, dtype=np.uint8)
+        self._check(self.L.gtd_dp_read_table(self._h, _ptr(out), nbytes))
+        return out, n, lb
+
+
+def table_index(n: int, tile_bits: int, subset_mask: int) -> int:
+    return int(load().gtd_dp_table_index(n, tile_bits, subset_mask))

@@ -1,0 +1,410 @@
+// C ABI of the gtd library: handles and the subset-DP entry points.
+// Errors never cross the ABI as exceptions; every call returns gtd_status and
+// keeps a message for gtd_last_error.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "gtd_device.cuh"
+#include "gtd_handle.h"
+
+namespace gtd {
+
+gtd_status fail(gtd_handle h, gtd_status s, const std::string& msg) {
+  if (h)
+    h->last_error = msg;
+  return s;
+}
+
+gtd_status cuda_fail(gtd_handle h, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(h, e == cudaErrorMemoryAllocation ? GTD_OOM : GTD_CUDA_ERROR, m);
+}
+
+namespace {
+
+// Makes the handle's device current for the duration of a call and restores
+// the caller's device afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess)
+      prev = -1;
+    if (prev != dev)
+      cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+      cudaSetDevice(prev);
+  }
+};
+
+#define GTD_CUDA(h, call)                         \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess)                        \
+      return ::gtd::cuda_fail((h), e_, #call);    \
+  } while (0)
+
+gtd_status check_adjacency(gtd_handle h, const uint64_t* adj, int n) {
+  const uint64_t allowed = n >= 64 ? ~0ull : ((1ull << n) - 1);
+  for (int v = 0; v < n; ++v) {
+    if ((adj[v] >> v) & 1ull)
+      return fail(h, GTD_INVALID_ARG, "Self loops are not allowed (vertex " + std::to_string(v) + ")");
+    if (adj[v] & ~allowed)
+      return fail(h, GTD_INVALID_ARG, "adjacency of vertex " + std::to_string(v) + " has a bit >= n");
+    for (uint64_t s = adj[v]; s; s &= s - 1) {
+      int u = __builtin_ctzll(s);
+      if (!((adj[u] >> v) & 1ull))
+        return fail(h, GTD_INVALID_ARG, "adjacency is not symmetric at (" + std::to_string(v) + ", " +
+                                            std::to_string(u) + ")");
+    }
+  }
+  return GTD_OK;
+}
+
+gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info) {
+  switch (code) {
+    case kDevOk:
+      return GTD_OK;
+    case kDevInvalidInput:
+      return fail(h, GTD_INVALID_ARG, "adjacency rejected on the device (self loop, bit >= n or asymmetric)");
+    case kDevWaitTimeout:
+      return fail(h, GTD_TIMEOUT, "a tile dependency wait exceeded its deadline");
+    case kDevNoRoot:
+      return fail(h, GTD_ABORTED, "tree reconstruction found no optimal root (info " + std::to_string(info) + ")");
+    case kDevDeadline:
+      return fail(h, GTD_TIMEOUT, "search deadline reached");
+    case kDevOverflow:
+      return fail(h, GTD_ABORTED, "a bounded device buffer overflowed (info " + std::to_string(info) + ")");
+    default:
+      return fail(h, GTD_ABORTED, "device error " + std::to_string(code));
+  }
+}
+
+int default_tile_bits(int n) {
+  (void)n;
+  return 10;
+}
+
+// Allocates (or grows) the table and flag buffers and enqueues the DP and
+// tree kernels. Outputs go to td/parent/order (device pointers, may be the
+// handle's IO block).
+gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_opts* opts,
+                      int32_t* d_td, int32_t* d_parent, int32_t* d_order) {
+  const int tile_bits = (opts && opts->tile_bits > 0) ? opts->tile_bits : default_tile_bits(n);
+  DpKernelParams p;
+  p.lay = make_dp_layout(n, tile_bits);
+  const size_t table_bytes = size_t(1) << n;
+  if (h->table_cap < table_bytes) {
+    if (h->d_table)
+      cudaFree(h->d_table);
+    h->d_table = nullptr;
+    h->table_cap = 0;
+    h->have_table = false;
+    GTD_CUDA(h, cudaMalloc(&h->d_table, table_bytes < 256 ? 256 : table_bytes));
+    h->table_cap = table_bytes < 256 ? 256 : table_bytes;
+  }
+  if (h->flags_cap < p.lay.ntiles) {
+    if (h->d_flags)
+      cudaFree(h->d_flags);
+    h->d_flags = nullptr;
+    h->flags_cap = 0;
+    GTD_CUDA(h, cudaMalloc(&h->d_flags, sizeof(uint32_t) * p.lay.ntiles));
+    GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * p.lay.ntiles, h->stream));
+    h->flags_cap = p.lay.ntiles;
+    h->epoch = 0;
+  }
+  if (++h->epoch == 0xffffffffu) {
+    GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * h->flags_cap, h->stream));
+    h->epoch = 1;
+  }
+  p.table = h->d_table;
+  p.flags = h->d_flags;
+  p.ticket = reinterpret_cast<uint32_t*>(h->d_io + kIoTicket);
+  p.error = h->d_io + kIoError;
+  p.adj = d_adj;
+  p.epoch = h->epoch;
+  p.timeout_ns = (opts && opts->timeout_ns) ? opts->timeout_ns : 10ull * 1000 * 1000 * 1000;
+
+  int occ = dp_tile_occupancy(p.lay.lb);
+  if (opts && opts->ctas_per_sm > 0 && opts->ctas_per_sm < occ)
+    occ = opts->ctas_per_sm;
+  if (occ < 1)
+    occ = 1;
+  long long ctas = static_cast<long long>(h->num_sms) * occ;
+  if (ctas > p.lay.ntiles)
+    ctas = p.lay.ntiles;
+
+  GTD_CUDA(h, cudaMemsetAsync(h->d_io, 0, 4 * sizeof(int32_t), h->stream));
+  GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  GTD_CUDA(h, dp_launch_tiles(p, static_cast<int>(ctas), h->stream));
+  GTD_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+  const uint64_t full = n == 64 ? ~0ull : ((1ull << n) - 1);
+  GTD_CUDA(h, dp_launch_tree(p, full, d_td, d_parent, d_order, h->stream));
+  GTD_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+
+  h->last_params = p;
+  h->have_table = true;
+  h->pending_stats = true;
+  gtd_dp_stats& st = h->last_stats;
+  st = gtd_dp_stats{};
+  st.table_bytes = table_bytes;
+  st.alg_bytes = table_bytes + static_cast<uint64_t>(n) * (table_bytes / 2);
+  st.tile_bits = p.lay.lb;
+  st.tiles = static_cast<int>(p.lay.ntiles);
+  st.ctas = static_cast<int>(ctas);
+  return GTD_OK;
+}
+
+void collect_stats(gtd_handle h) {
+  if (!h->pending_stats)
+    return;
+  float a = 0, b = 0;
+  if (cudaEventElapsedTime(&a, h->ev[0], h->ev[1]) == cudaSuccess)
+    h->last_stats.dp_ms = a;
+  if (cudaEventElapsedTime(&b, h->ev[1], h->ev[2]) == cudaSuccess)
+    h->last_stats.tree_ms = b;
+  h->pending_stats = false;
+}
+
+}  // namespace
+}  // namespace gtd
+
+using namespace gtd;
+
+extern "C" {
+
+const char* gtd_status_string(gtd_status s) {
+  switch (s) {
+    case GTD_OK: return "GTD_OK";
+    case GTD_INVALID_ARG: return "GTD_INVALID_ARG";
+    case GTD_NOT_CONNECTED: return "GTD_NOT_CONNECTED";
+    case GTD_OOM: return "GTD_OOM";
+    case GTD_TIMEOUT: return "GTD_TIMEOUT";
+    case GTD_ABORTED: return "GTD_ABORTED";
+    case GTD_CUDA_ERROR: return "GTD_CUDA_ERROR";
+    case GTD_NO_RESULT: return "GTD_NO_RESULT";
+  }
+  return "GTD_UNKNOWN";
+}
+
+const char* gtd_last_error(gtd_handle h) { return h ? h->last_error.c_str() : "null handle"; }
+
+gtd_status gtd_create(gtd_handle* out, int device, void* stream) {
+  if (!out)
+    return GTD_INVALID_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+    return GTD_CUDA_ERROR;
+  if (device < 0 || device >= count)
+    return GTD_INVALID_ARG;
+  gtd_handle h = new (std::nothrow) gtd_handle_s();
+  if (!h)
+    return GTD_OOM;
+  DeviceGuard g(device);
+  h->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) {
+    if (stream) {
+      h->stream = static_cast<cudaStream_t>(stream);
+    } else {
+      e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+      h->own_stream = true;
+    }
+  }
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+    e = cudaEventCreate(&h->ev[i]);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->d_io, kIoWords * sizeof(int32_t));
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->d_adj, kDpMaxN * sizeof(uint64_t));
+  if (e == cudaSuccess)
+    e = cudaMallocHost(&h->h_pinned, 4096);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->d_io, 0, kIoWords * sizeof(int32_t), h->stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    gtd_destroy(h);
+    return e == cudaErrorMemoryAllocation ? GTD_OOM : GTD_CUDA_ERROR;
+  }
+  *out = h;
+  return GTD_OK;
+}
+
+gtd_status gtd_destroy(gtd_handle h) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  {
+    DeviceGuard g(h->device);
+    if (h->stream)
+      cudaStreamSynchronize(h->stream);
+    cudaFree(h->d_table);
+    cudaFree(h->d_flags);
+    cudaFree(h->d_io);
+    cudaFree(h->d_adj);
+    if (h->h_pinned)
+      cudaFreeHost(h->h_pinned);
+    for (auto& e : h->ev)
+      if (e)
+        cudaEventDestroy(e);
+    if (h->own_stream && h->stream)
+      cudaStreamDestroy(h->stream);
+  }
+  delete h;
+  return GTD_OK;
+}
+
+gtd_status gtd_dp_solve(gtd_handle h, const uint64_t* adj, int n, int32_t* td_out,
+                        int32_t* parent_out, int32_t* order_out, const gtd_dp_opts* opts,
+                        gtd_dp_stats* stats) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!adj || !td_out || !parent_out)
+    return fail(h, GTD_INVALID_ARG, "null pointer argument");
+  if (n < 1 || n > GTD_DP_MAX_N)
+    return fail(h, GTD_INVALID_ARG, "n must be in [1, " + std::to_string(GTD_DP_MAX_N) + "]");
+  gtd_status s = check_adjacency(h, adj, n);
+  if (s != GTD_OK)
+    return s;
+  const auto t0 = std::chrono::steady_clock::now();
+  DeviceGuard g(h->device);
+  if (n == 1) {
+    *td_out = 1;
+    parent_out[0] = -1;
+    if (order_out)
+      order_out[0] = 0;
+    h->have_table = false;
+    if (stats)
+      *stats = gtd_dp_stats{};
+    return GTD_OK;
+  }
+  uint64_t* h_adj = static_cast<uint64_t*>(h->h_pinned);
+  std::memcpy(h_adj, adj, sizeof(uint64_t) * n);
+  GTD_CUDA(h, cudaMemcpyAsync(h->d_adj, h_adj, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, h->stream));
+  s = dp_enqueue(h, h->d_adj, n, opts, h->d_io + kIoTd, h->d_io + kIoParent, h->d_io + kIoOrder);
+  if (s != GTD_OK)
+    return s;
+  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
+  GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, (kIoOrder + 64) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                              h->stream));
+  GTD_CUDA(h, cudaStreamSynchronize(h->stream));
+  collect_stats(h);
+  s = map_device_error(h, h_io[kIoError], h_io[kIoError + 1]);
+  if (s != GTD_OK) {
+    h->have_table = false;
+    return s;
+  }
+  *td_out = h_io[kIoTd];
+  std::memcpy(parent_out, h_io + kIoParent, sizeof(int32_t) * n);
+  if (order_out)
+    std::memcpy(order_out, h_io + kIoOrder, sizeof(int32_t) * n);
+  h->last_stats.total_ms =
+      std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats)
+    *stats = h->last_stats;
+  return GTD_OK;
+}
+
+gtd_status gtd_dp_solve_device(gtd_handle h, const uint64_t* d_adj, int n, int32_t* d_td,
+                               int32_t* d_parent, int32_t* d_order, const gtd_dp_opts* opts) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!d_adj || !d_td || !d_parent)
+    return fail(h, GTD_INVALID_ARG, "null pointer argument");
+  if (n < 2 || n > GTD_DP_MAX_N)
+    return fail(h, GTD_INVALID_ARG, "device solve needs n in [2, " + std::to_string(GTD_DP_MAX_N) + "]");
+  DeviceGuard g(h->device);
+  return dp_enqueue(h, d_adj, n, opts, d_td, d_parent, d_order);
+}
+
+gtd_status gtd_sync(gtd_handle h, gtd_dp_stats* stats) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  DeviceGuard g(h->device);
+  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
+  GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  GTD_CUDA(h, cudaStreamSynchronize(h->stream));
+  collect_stats(h);
+  if (stats)
+    *stats = h->last_stats;
+  gtd_status s = map_device_error(h, h_io[kIoError], h_io[kIoError + 1]);
+  if (s != GTD_OK)
+    h->have_table = false;
+  return s;
+}
+
+gtd_status gtd_dp_query(gtd_handle h, uint64_t subset_mask, int32_t* td_out, int32_t* order_out) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!h->have_table)
+    return fail(h, GTD_NO_RESULT, "no DP table: solve a graph first");
+  const int n = h->last_params.lay.n;
+  if (n < 64 && (subset_mask >> n))
+    return fail(h, GTD_INVALID_ARG, "subset has a vertex >= n");
+  if (!td_out)
+    return fail(h, GTD_INVALID_ARG, "null td_out");
+  DeviceGuard g(h->device);
+  GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoError, 0, 2 * sizeof(int32_t), h->stream));
+  GTD_CUDA(h, dp_launch_tree(h->last_params, subset_mask, h->d_io + kIoTd, nullptr,
+                             order_out ? h->d_io + kIoOrder : nullptr, h->stream));
+  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
+  GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, (kIoOrder + 64) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                              h->stream));
+  GTD_CUDA(h, cudaStreamSynchronize(h->stream));
+  gtd_status s = map_device_error(h, h_io[kIoError], h_io[kIoError + 1]);
+  if (s != GTD_OK)
+    return s;
+  *td_out = h_io[kIoTd];
+  if (order_out)
+    std::memcpy(order_out, h_io + kIoOrder, sizeof(int32_t) * __builtin_popcountll(subset_mask));
+  return GTD_OK;
+}
+
+gtd_status gtd_dp_table(gtd_handle h, const uint8_t** d_table, uint64_t* bytes, int* n, int* tile_bits) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!h->have_table)
+    return fail(h, GTD_NO_RESULT, "no DP table: solve a graph first");
+  if (d_table)
+    *d_table = h->d_table;
+  if (bytes)
+    *bytes = uint64_t(1) << h->last_params.lay.n;
+  if (n)
+    *n = h->last_params.lay.n;
+  if (tile_bits)
+    *tile_bits = h->last_params.lay.lb;
+  return GTD_OK;
+}
+
+gtd_status gtd_dp_read_table(gtd_handle h, uint8_t* out, uint64_t bytes) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!h->have_table)
+    return fail(h, GTD_NO_RESULT, "no DP table: solve a graph first");
+  const uint64_t need = uint64_t(1) << h->last_params.lay.n;
+  if (!out || bytes < need)
+    return fail(h, GTD_INVALID_ARG, "output buffer smaller than the table");
+  DeviceGuard g(h->device);
+  GTD_CUDA(h, cudaMemcpyAsync(out, h->d_table, need, cudaMemcpyDeviceToHost, h->stream));
+  GTD_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GTD_OK;
+}
+
+uint64_t gtd_dp_table_index(int n, int tile_bits, uint64_t subset_mask) {
+  if (n < 2 || n > GTD_DP_MAX_N)
+    return ~0ull;
+  DpLayout L = make_dp_layout(n, tile_bits);
+  if (L.lb != tile_bits)
+    return ~0ull;
+  return L.index(subset_mask);
+}
+
+}  // extern "C"

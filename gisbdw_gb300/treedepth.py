@@ -1,0 +1,101 @@
+"""Reference-shaped solver classes over the gtd C ABI.
+
+Mirrors the reference's algorithm interface (Treedepth/src): a solver object
+is called on a graph and hands back the treedepth and an elimination tree.
+
+* :class:`DynamicGPU` — ``td::DynamicGPU`` (dynamic_gpu.hpp:17-37):
+  ``solver(g)`` runs the subset DP; ``GetElimination(nverts, subset_size,
+  subset_code)`` returns the elimination order of the subset with that colex
+  rank (dynamic_gpu.hpp:48-64); :meth:`Result` gives the
+  ``EliminationTree::Result``-shaped output (elimination_tree.hpp:26-30).
+
+Errors map to the reference's exception types: invalid input raises
+``InvalidArgument`` (a ``ValueError``, the reference's
+``std::invalid_argument``).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from .graphs import Graph
+
+
+@dataclass
+class Result:
+    """``EliminationTree::Result`` (elimination_tree.hpp:26-30): the tree as
+    a parent array (``parent[root] == -1``), its height ``treedepth`` and
+    ``root``. ``td_decomp`` lists the tree edges (parent, child)."""
+
+    treedepth: int
+    root: int
+    parent: np.ndarray
+
+    @property
+    def td_decomp(self) -> List[Tuple[int, int]]:
+        return [(int(p), v) for v, p in enumerate(self.parent) if p >= 0]
+
+
+def _masks(g: Graph) -> np.ndarray:
+    return g.adj64()
+
+
+def _decode(nverts: int, k: int, code: int) -> int:
+    """Colex unrank (set_encoder.hpp:61-73) to a bit mask."""
+    from math import comb
+    mask = 0
+    while k > 0:
+        nverts -= 1
+        c = comb(nverts, k)
+        if code >= c:
+            mask |= 1 << nverts
+            code -= c
+            k -= 1
+    return mask
+
+
+class DynamicGPU:
+    """Exact treedepth by the GB300 subset DP (``td::DynamicGPU``)."""
+
+    def __init__(self, device: int = 0, tile_bits: int = 0, handle: Optional[_lib.Handle] = None):
+        self._h = handle or _lib.Handle(device)
+        self._tile_bits = tile_bits
+        self._n = 0
+        self._td = None
+        self._parent = None
+        self._order = None
+        self.stats: dict = {}
+
+    def __call__(self, g: Graph) -> None:
+        if g.n > _lib.DP_MAX_N:
+            raise _lib.InvalidArgument(1, f"subset DP supports n <= {_lib.DP_MAX_N}")
+        td, parent, order, stats = self._h.dp_solve(_masks(g), g.n, tile_bits=self._tile_bits)
+        self._n, self._td, self._parent, self._order, self.stats = g.n, td, parent, order, stats
+
+    @property
+    def treedepth(self) -> int:
+        if self._td is None:
+            raise _lib.GtdError(7, "no solve yet")
+        return self._td
+
+    def Result(self) -> Result:
+        if self._td is None:
+            raise _lib.GtdError(7, "no solve yet")
+        roots = np.flatnonzero(self._parent == -1)
+        return Result(self._td, int(roots[0]) if len(roots) else -1, self._parent.copy())
+
+    def GetElimination(self, nverts: int, subset_size: int, subset_code: int) -> List[int]:
+        """Elimination order of the subset of rank ``subset_code`` among the
+        ``subset_size``-subsets of ``nverts`` vertices (dynamic_gpu.hpp:48-64).
+        The full vertex set is (n, n, 0)."""
+        if subset_size == nverts == self._n and subset_code == 0 and self._order is not None:
+            return self._order.tolist()
+        td, order = self._h.dp_query(_decode(nverts, subset_size, subset_code))
+        return order
+
+    def GetTreedepth(self, subset_mask: int) -> int:
+        td, _ = self._h.dp_query(subset_mask, want_order=False)
+        return td

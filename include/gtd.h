@@ -1,0 +1,115 @@
+/* gtd — GB300-native exact treedepth solvers, C ABI.
+ *
+ * Drop-in boundary for the exact solvers of Zackere/GiSBDW (Treedepth/src):
+ * a graph goes in, its exact treedepth and an elimination tree come out.
+ * Every entry point takes plain pointers and sizes, never throws, and returns
+ * a gtd_status. The C++ layer in include/gtd/treedepth.hpp maps these codes
+ * to the exception types the reference throws.
+ *
+ * Graphs: n vertices 0..n-1, adjacency as bit masks. adj[v] has bit u set iff
+ * the undirected edge uv exists; masks must be symmetric with no self loops.
+ * Trees: parent[v] is v's parent in the elimination tree, -1 for the root
+ * (roots, for a disconnected graph's elimination forest). The tree height
+ * (counted in vertices) equals the treedepth.
+ *
+ * Threading: a handle owns its device buffers and one CUDA stream; it is not
+ * thread-safe. Use one handle per host thread.
+ */
+#ifndef GTD_H_
+#define GTD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GTD_OK = 0,
+  GTD_INVALID_ARG = 1, /* n out of range, self loop, asymmetric masks, bad pointer */
+  GTD_NOT_CONNECTED = 2, /* input must be connected (branch and bound) */
+  GTD_OOM = 3,           /* device allocation failed */
+  GTD_TIMEOUT = 4,       /* a bounded wait or a deadline ran out */
+  GTD_ABORTED = 5,       /* stopped by gtd_abort or another error */
+  GTD_CUDA_ERROR = 6,    /* a CUDA runtime call failed */
+  GTD_NO_RESULT = 7      /* query before a solve, or subset not available */
+} gtd_status;
+
+typedef struct gtd_handle_s* gtd_handle;
+
+/* Largest n the subset DP accepts (table of 2^n bytes: 64 GiB at n = 36). */
+#define GTD_DP_MAX_N 36
+
+/* Creates a handle on CUDA device `device`. `stream` is a cudaStream_t to
+ * run on, or NULL for a handle-owned stream. */
+gtd_status gtd_create(gtd_handle* out, int device, void* stream);
+gtd_status gtd_destroy(gtd_handle h);
+const char* gtd_status_string(gtd_status s);
+/* Human-readable detail of the last failure on this handle. */
+const char* gtd_last_error(gtd_handle h);
+
+/* Options and statistics of one subset-DP solve. */
+typedef struct {
+  int tile_bits;        /* low vertices per tile (0 = autotuned default) */
+  int ctas_per_sm;      /* persistent CTAs per SM (0 = default) */
+  uint64_t timeout_ns;  /* bound on every in-kernel wait (0 = 10 s) */
+} gtd_dp_opts;
+
+typedef struct {
+  float dp_ms;          /* DP kernel time, CUDA events on the handle's stream */
+  float tree_ms;        /* tree reconstruction kernel */
+  float total_ms;       /* whole call including copies */
+  uint64_t table_bytes; /* 2^n */
+  uint64_t alg_bytes;   /* 2^n + n 2^(n-1): one write + |S| one-byte gathers per subset */
+  int tile_bits;
+  int tiles;
+  int ctas;
+} gtd_dp_stats;
+
+/* DynamicGPU (Treedepth/src/dynamic_gpu/dynamic_gpu.cu:171-201 Run, with
+ * the reconstruction of dynamic_gpu.hpp:48-64 GetElimination and
+ * main.cpp:187-195): exact treedepth of the graph and the elimination tree
+ * whose every connected component is rooted at its first vertex v with
+ * td(C - v) = td(C) - 1 (the reference's first-argmin root,
+ * dynamic_gpu.cu:84-87). Host pointers: adj[n] in, td_out, parent_out[n]
+ * and, if non-null, order_out[n] (the reference's GetElimination order) out.
+ * The DP table stays on the device for gtd_dp_query until the next solve.
+ * 1 <= n <= GTD_DP_MAX_N; disconnected graphs give an elimination forest. */
+gtd_status gtd_dp_solve(gtd_handle h, const uint64_t* adj, int n,
+                        int32_t* td_out, int32_t* parent_out,
+                        int32_t* order_out, const gtd_dp_opts* opts,
+                        gtd_dp_stats* stats);
+
+/* Same computation with adjacency, td, parent and order in DEVICE memory;
+ * enqueued on the handle's stream without a host synchronisation (stats and
+ * errors are collected by gtd_sync). order_out may be NULL. */
+gtd_status gtd_dp_solve_device(gtd_handle h, const uint64_t* d_adj, int n,
+                               int32_t* d_td, int32_t* d_parent,
+                               int32_t* d_order, const gtd_dp_opts* opts);
+
+/* Waits for the handle's stream; reports in-kernel errors (timeouts) of
+ * device-side solves and fills stats of the last DP solve if non-null. */
+gtd_status gtd_sync(gtd_handle h, gtd_dp_stats* stats);
+
+/* DynamicGPU::GetElimination (dynamic_gpu.hpp:48-64) on the table of the
+ * last solve: treedepth of the subset `subset_mask` and its elimination
+ * order (order_out[popcount(subset_mask)]; NULL to skip). */
+gtd_status gtd_dp_query(gtd_handle h, uint64_t subset_mask, int32_t* td_out,
+                        int32_t* order_out);
+
+/* Device pointer and size of the last solve's table (for inspection in
+ * tests): entry of subset S lives at gtd_dp_table_index(n, tile_bits, S).
+ * Each byte holds td in bits 0-5 and a "connected" flag in bit 7. */
+gtd_status gtd_dp_table(gtd_handle h, const uint8_t** d_table, uint64_t* bytes,
+                        int* n, int* tile_bits);
+uint64_t gtd_dp_table_index(int n, int tile_bits, uint64_t subset_mask);
+
+/* Copies the last solve's table (2^n bytes, tiled layout as above) to host
+ * memory `out` of `bytes` bytes. */
+gtd_status gtd_dp_read_table(gtd_handle h, uint8_t* out, uint64_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GTD_H_ */

@@ -220,6 +220,41 @@ int gtdo_tree_from_table(int n, const uint64_t* adj, const uint8_t* T, int* td,
   return 0;
 }
 
+/* Root of a connected set: first v with T[C \ v] = T[C] - 1. */
+static int first_root(uint64_t C, const uint8_t* T) {
+  if (pop64(C) == 1)
+    return ctz64(C);
+  uint8_t want = (uint8_t)(T[C] - 1);
+  for (uint64_t s = C; s; s &= s - 1)
+    if (T[C & ~(1ull << ctz64(s))] == want)
+      return ctz64(s);
+  return -1;
+}
+
+int gtdo_get_elimination(int n, const uint64_t* adj, const uint8_t* T,
+                         uint64_t subset, int* order) {
+  (void)n;
+  int step = 0;
+  while (subset) {
+    uint64_t best = 0;
+    uint8_t best_td = 0;
+    for (uint64_t rest = subset; rest;) {
+      uint64_t c = component64(rest, ctz64(rest), adj);
+      rest &= ~c;
+      if (!best || T[c] > best_td) {
+        best = c;
+        best_td = T[c];
+      }
+    }
+    int r = first_root(best, T);
+    if (r < 0)
+      return -1;
+    order[step++] = r;
+    subset &= ~(1ull << r);
+  }
+  return 0;
+}
+
 int gtdo_dp_solve(int n, const uint64_t* adj, int nthreads, int* td,
                   int* parent) {
   if (n < 1 || n > 34)

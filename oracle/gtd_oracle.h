@@ -50,6 +50,13 @@ int gtdo_dp_table(int n, const uint64_t* adj, uint8_t* table, int nthreads);
 int gtdo_tree_from_table(int n, const uint64_t* adj, const uint8_t* table,
                          int* td, int* parent);
 
+/* DynamicGPU::GetElimination (dynamic_gpu.hpp:48-64) on a bit-mask-indexed
+ * table: repeatedly remove the stored root of the remaining set, which for a
+ * disconnected set is the root of its first deepest component
+ * (dynamic_gpu.cu:92-103). Writes popcount(subset) vertices; returns 0. */
+int gtdo_get_elimination(int n, const uint64_t* adj, const uint8_t* table,
+                         uint64_t subset, int* order);
+
 /* gtdo_dp_table + gtdo_tree_from_table with an internally allocated table.
  * Returns 0, -1 bad n, -2 out of memory. */
 int gtdo_dp_solve(int n, const uint64_t* adj, int nthreads, int* td,

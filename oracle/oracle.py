@@ -58,6 +58,7 @@ class Port:
         L.gtdo_edge_lower_bound.argtypes = [_i, _i]
         L.gtdo_dp_table.argtypes = [_i, _vp, _vp, _i]
         L.gtdo_tree_from_table.argtypes = [_i, _vp, _vp, _ip, _vp]
+        L.gtdo_get_elimination.argtypes = [_i, _vp, _vp, _u64, _vp]
         L.gtdo_dp_solve.argtypes = [_i, _vp, _i, _ip, _vp]
         L.gtdo_dp_improv.argtypes = [_i, _vp, _ip, _vp, ctypes.POINTER(_i64)]
         L.gtdo_elimination_tree.argtypes = [_i, _vp, _vp, _ip, _vp]
@@ -97,6 +98,14 @@ class Port:
         if rc:
             raise ValueError(f"gtdo_tree_from_table rc={rc}")
         return td.value, par
+
+    def get_elimination(self, g, T: np.ndarray, subset: int) -> List[int]:
+        adj = g.adj64()
+        out = np.zeros(max(1, bin(subset).count("1")), dtype=np.int32)
+        rc = self.L.gtdo_get_elimination(g.n, _ptr(adj), _ptr(T), subset, _ptr(out))
+        if rc:
+            raise ValueError(f"gtdo_get_elimination rc={rc}")
+        return out[:bin(subset).count("1")].tolist()
 
     def dp_solve(self, g, nthreads: int = 1) -> Tuple[int, np.ndarray]:
         adj = g.adj64()
