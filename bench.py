@@ -1,0 +1,340 @@
+"""Benchmark: exact treedepth solves on GB300.
+
+Workload (default, ``--workload dp-c2``): the single-graph subset DP at scale,
+8 connected G(n, p) graphs (n in {28, 30, 32}, p in {0.1, 0.2, 0.3}, seeds
+1-8) plus the 5 x 6 grid. One step solves all 9 graphs exactly (DP table +
+elimination tree). The DP tables (256 MiB - 4 GiB) are larger than L2, so no
+flush is needed between steps.
+
+Arms:
+  default            gtd on the GPU; ``value`` = solves/s with inputs resident
+                     on the device; ``e2e`` = the same through the host-buffer
+                     C-ABI call gtd_dp_solve (H2D/D2H copies inside the timed
+                     region).
+  --impl reference   the reference's CPU algorithm (the oracle restatement of
+                     DynamicGPU's recurrence, dynamic_gpu.cu:68-112, on all
+                     host threads), each step one graph of a bounded sample.
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "exact-treedepth solves/s & p50 time-to-proof: learned-guided vs plain GPU B&B"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gtd", choices=["gtd", "reference"])
+    ap.add_argument("--workload", default="dp-c2", choices=["dp-c2"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-n", type=int, default=0,
+                    help="restrict the workload to its graphs with this n (profiling)")
+    ap.add_argument("--tile-bits", type=int, default=0,
+                    help="DP tile bits (0 = the library's default)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the DP tile kernel from the committed ncu
+    summary (profiles/dp_tile_kernel.md, line 'dram_bytes_per_launch_n30')."""
+    path = os.path.join(ROOT, "profiles", "dp_tile_kernel.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch_n30:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle is loaded only here).
+# ---------------------------------------------------------------------------
+
+def cpu_sample_graphs(graphs):
+    return [g for g in graphs if g.n == 28]
+
+
+def time_cpu_dp(graphs, steps, threads):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    port = oracle.Port()
+    times, tds = [], []
+    for i in range(steps):
+        g = graphs[i % len(graphs)]
+        t0 = time.perf_counter()
+        td, _ = port.dp_solve(g, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+        tds.append(td)
+    return times, tds
+
+
+def run_reference(args, graphs):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = cpu_sample_graphs(graphs)
+    time_cpu_dp(sample, args.warmup, threads)
+    times, _ = time_cpu_dp(sample, args.steps, threads)
+    total = sum(times)
+    value = len(times) / total
+    desc = (f"n=28 graphs of the workload ({', '.join(g.name for g in sample)}), one per step, "
+            f"oracle restatement of DynamicGPU's all-subsets recurrence on {threads} host threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "dp-c2 (config 2: 8 G(n,p) n in {28,30,32} + grid 5x6)",
+                   "sample": "n=28 graphs only"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": desc, "cpu": cpu_model()},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm.
+# ---------------------------------------------------------------------------
+
+def run_gpu(args, graphs):
+    import numpy as np
+    import torch
+
+    from gisbdw_gb300 import Handle
+    from gisbdw_gb300.validate import check_tree
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    # The library runs on this torch stream, so the CUDA events below bracket
+    # its kernels on the stream they are launched on.
+    stream = torch.cuda.Stream()
+    h = Handle(local, stream=stream.cuda_stream)
+
+    d_adj = [torch.from_numpy(g.adj64().view(np.int64)).cuda() for g in graphs]
+    d_td = torch.zeros(len(graphs), dtype=torch.int32, device="cuda")
+    d_par = torch.zeros((len(graphs), 64), dtype=torch.int32, device="cuda")
+
+    def step():
+        st = []
+        for i, g in enumerate(graphs):
+            h.dp_solve_device(d_adj[i].data_ptr(), g.n, d_td[i:].data_ptr(), d_par[i].data_ptr(),
+                              tile_bits=args.tile_bits)
+            st.append(h.sync())
+        return st
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    # correctness of what the timed loop computes (tree valid, height = td)
+    tds = d_td.cpu().tolist()
+    pars = d_par.cpu().numpy()
+    for i, g in enumerate(graphs):
+        if not check_tree(g, tds[i], pars[i, :g.n]):
+            raise SystemExit(f"invalid elimination tree for {g.name}")
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    kstats = []
+    for _ in range(args.steps):
+        kstats.extend(step())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    clocks = sampler.stop()
+    if world > 1:
+        t = torch.tensor([elapsed_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    solves = len(graphs) * args.steps * world
+    value = solves / (elapsed_ms / 1000.0)
+
+    # e2e: host buffers through the C ABI call (adjacency H2D, results D2H)
+    e2e_times = []
+    h2d = sum(8 * g.n for g in graphs)
+    d2h = len(graphs) * (136 * 4)
+    adjs = [g.adj64() for g in graphs]
+    for _ in range(max(1, args.warmup // 2)):
+        for i, g in enumerate(graphs):
+            h.dp_solve(adjs[i], g.n, tile_bits=args.tile_bits)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for i, g in enumerate(graphs):
+            td, par, order, _ = h.dp_solve(adjs[i], g.n, tile_bits=args.tile_bits)
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_value = len(graphs) * args.steps * world / e2e_s
+
+    # roofline of the dominant kernel (dp_tile_kernel), from live events
+    alg = sum(s["alg_bytes"] for s in kstats)
+    kms = sum(s["dp_ms"] for s in kstats)
+    launches = len(kstats)
+    peak, peak_kind = peaks()
+    achieved = alg / (kms / 1000.0) / 1e9
+    per_graph_ms = [s["dp_ms"] + s["tree_ms"] for s in kstats[-len(graphs):]]
+    by_n = {}
+    for g, s in zip(graphs * args.steps, kstats):
+        by_n.setdefault(g.n, []).append(s)
+    by_n_out = {str(n): {"dp_ms": statistics.median(x["dp_ms"] for x in v),
+                         "alg_GBps": statistics.median(x["alg_bytes"] / (x["dp_ms"] / 1e3) / 1e9 for x in v)}
+                for n, v in sorted(by_n.items())}
+    traffic = ncu_traffic()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic",
+        "config": {"workload": "dp-c2 (config 2: 8 connected G(n,p), n in {28,30,32}, p in {0.1,0.2,0.3}, "
+                               "seeds 1-8, + grid 5x6; exact DP + elimination tree per graph)",
+                   "graphs": [g.name for g in graphs], "l2": "working set (DP tables 256 MiB-4 GiB) > L2",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "p50_time_to_proof_ms": statistics.median(per_graph_ms),
+        "treedepths": tds,
+        "roofline": {"bound": "hbm", "kernel": "dp_tile_kernel", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "alg_bytes_per_launch_mean": alg / launches,
+                     "launch_ms_mean": kms / launches, "by_n": by_n_out},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = cpu_sample_graphs(graphs)
+        times, ctds = time_cpu_dp(sample, len(sample), threads)
+        gpu_td = {g.name: tds[i] for i, g in enumerate(graphs)}
+        line["cpu_baseline"] = {
+            "value": len(times) / sum(times), "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sample)} n=28 graphs of the workload, oracle restatement of DynamicGPU's "
+                      f"recurrence on {threads} host threads ({cpu_model()})",
+            "td_agree": all(gpu_td[g.name] == t for g, t in zip(sample, ctds))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    from gisbdw_gb300 import graphs as G
+    graphs = G.config2_graphs()
+    if args.only_n:
+        graphs = [g for g in graphs if g.n == args.only_n]
+    if args.impl == "reference":
+        run_reference(args, graphs)
+    else:
+        run_gpu(args, graphs)
+
+
+if __name__ == "__main__":
+    main()

@@ -15,18 +15,21 @@
 //      T[S] = 1 + min_v T[S - v]   (connected; dynamic_gpu.cu:68-89)
 //      T[S] = max_v T[S - v]       (disconnected; = max over components,
 //                                   dynamic_gpu.cu:90-111)
-//    with the connected flag kept in bit 7 of each table byte. No per-subset
-//    BFS, no ranking per child.
+//    with each table byte holding td << 1 | connected. No per-subset BFS, no
+//    ranking per child.
 //  * Layout (gtd_dp_layout.h). Tiles of 2^lb subsets share a high part H;
 //    a tile's cross-tile children are the whole tiles H - h one level down,
-//    read as contiguous 2^lb-byte blocks; the in-tile children are resolved
-//    in shared memory in popcount order of the low part.
-//  * Schedule. One persistent launch: CTAs take tiles by ticket (atomicAdd)
-//    in level-major order, wait on per-tile ready flags of the |H| child
-//    tiles (each wait bounded by a deadline), reduce the children with 4-way
-//    SIMD byte min/max, resolve the tile, store it, publish its flag. A tile
-//    only waits on tiles with smaller tickets, and a ticket is only taken by
-//    a running CTA, so the smallest unfinished ticket can always proceed.
+//    read as contiguous 2^lb-byte blocks (16-byte vector loads through L2);
+//    the in-tile children are resolved in shared memory, 4 subsets per
+//    32-bit word, words in popcount order of the word index.
+//  * Schedule. One persistent launch; every warp is an independent tile
+//    worker (no CTA barriers in the loop). A warp takes a tile by ticket
+//    (atomicAdd) in level-major order, its lanes wait on the ready flags of
+//    the |H| child tiles (each wait bounded by a deadline), the warp reduces
+//    the children with 4-way SIMD byte min/max, resolves the tile, stores it
+//    and publishes its flag. A tile only waits on tiles with smaller tickets,
+//    and a ticket is only taken by a running warp, so the smallest unfinished
+//    ticket can always proceed.
 //
 // Reconstruction (dp_tree_kernel): one warp, one lane per vertex, rebuilds
 // the reference's tree (first-argmin root per component, dynamic_gpu.cu:84-87,
@@ -40,11 +43,18 @@
 
 namespace gtd {
 
+// One warp resolves one tile; a CTA holds kDpWarps independent tile workers
+// that share only the adjacency and the word order table.
+constexpr int kDpWarps = 4;
+
 template <int LB>
 struct TileShape {
   static constexpr int kEntries = 1 << LB;
-  static constexpr int kWords = kEntries / 4;
-  static constexpr int kThreads = kWords < 32 ? 32 : kWords;
+  static constexpr int kWords = kEntries / 4;   // 4 subsets per 32-bit word
+  static constexpr int kWordBits = LB - 2;
+  // dynamic shared memory: per warp T, A, B (kWords words each), then the
+  // shared word order (kWords uint16) and the adjacency (kDpMaxN uint64).
+  static constexpr size_t kSmem = size_t(kDpWarps) * 3 * kWords * 4 + kWords * 2 + 16 + kDpMaxN * 8;
 };
 
 // Checks the adjacency masks: no self loop, no bit >= n, symmetric.
@@ -65,43 +75,72 @@ __device__ __forceinline__ bool adjacency_ok(const uint64_t* adj, int n) {
   return true;
 }
 
+// Table bytes hold td << 1 | connected, so an unsigned byte min (max) over
+// children gives 2 * min td (2 * max td) plus a flag bit, without masking.
+// Value of one subset from the min/max raw child bytes m, M, the number c of
+// connected children and k = |S|; s2 is S itself (used only when k == 2).
+__device__ __forceinline__ uint32_t resolve(uint32_t m, uint32_t M, uint32_t c, int k, uint64_t s2,
+                                            const uint64_t* adj) {
+  if (k <= 1)
+    return k == 0 ? 0u : 3u;  // empty set: td 0; singleton: td 1, connected
+  bool conn;
+  if (k == 2) {
+    const int u = __ffsll(static_cast<long long>(s2)) - 1;
+    const int v = 63 - __clzll(static_cast<long long>(s2));
+    conn = (adj[u] >> v) & 1ull;
+  } else {
+    conn = c >= 2u;  // >= 2 non-cut vertices <=> connected (|S| >= 3)
+  }
+  return conn ? ((m & ~1u) + 3u) : (M & ~1u);
+}
+
+__device__ __forceinline__ void acc_word(uint32_t x, uint32_t& mn, uint32_t& mx, uint32_t& ct) {
+  mn = __vminu4(mn, x);
+  mx = __vmaxu4(mx, x);
+  ct += x & 0x01010101u;
+}
+
+// Packs the cross-tile aggregates of one word: A = min raw | 0x80 where
+// >= 1 connected child, B = max raw | 0x80 where >= 2 connected children.
+__device__ __forceinline__ void pack_agg(uint32_t mn, uint32_t mx, uint32_t ct, uint32_t& a, uint32_t& b) {
+  a = (mn & 0x7F7F7F7Fu) | (__vcmpgtu4(ct, 0u) & 0x80808080u);
+  b = (mx & 0x7F7F7F7Fu) | (__vcmpgtu4(ct, 0x01010101u) & 0x80808080u);
+}
+
 template <int LB>
-__global__ void __launch_bounds__(TileShape<LB>::kThreads)
+__global__ void __launch_bounds__(32 * kDpWarps)
     dp_tile_kernel(const DpKernelParams p) {
   using Shape = TileShape<LB>;
-  constexpr int kEntries = Shape::kEntries;
   constexpr int kWords = Shape::kWords;
-  constexpr int kThreads = Shape::kThreads;
+  constexpr int kWordBits = Shape::kWordBits;
 
-  __shared__ uint32_t sT[kWords];
-  __shared__ uint32_t sMin[kWords];
-  __shared__ uint32_t sMax[kWords];
-  __shared__ uint32_t sCnt[kWords];
-  __shared__ uint16_t sOrder[kEntries];
-  __shared__ uint64_t sAdj[kDpMaxN];
-  __shared__ uint32_t sChild[kDpMaxHigh];
-  __shared__ uint32_t sTile;
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  uint32_t* T = reinterpret_cast<uint32_t*>(smem) + size_t(warp) * 3 * kWords;
+  uint32_t* A = T + kWords;
+  uint32_t* B = A + kWords;
+  uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + size_t(kDpWarps) * 3 * kWords * 4);
+  uint64_t* sAdj = reinterpret_cast<uint64_t*>(smem + ((size_t(kDpWarps) * 3 * kWords * 4 + kWords * 2 + 15) & ~size_t(15)));
   __shared__ int sBadInput;
 
-  const int tid = threadIdx.x;
   const DpLayout& lay = p.lay;
   const int n = lay.n;
-
-  for (int v = tid; v < n; v += kThreads)
+  for (int v = threadIdx.x; v < n; v += blockDim.x)
     sAdj[v] = p.adj[v];
-  // Low parts ordered by popcount, colex rank inside each popcount class.
-  for (int L = tid; L < kEntries; L += kThreads) {
-    const int i = __popc(L);
+  // Word indices ordered by popcount, colex rank inside each popcount class.
+  for (int w = threadIdx.x; w < kWords; w += blockDim.x) {
+    const int i = __popc(w);
     uint32_t pos = 0;
     for (int q = 0; q < i; ++q)
-      pos += lay.binom[LB][q];
+      pos += lay.binom[kWordBits][q];
     int m = 0;
-    for (uint32_t r = static_cast<uint32_t>(L); r; r &= r - 1)
+    for (uint32_t r = static_cast<uint32_t>(w); r; r &= r - 1)
       pos += lay.binom[__ffs(r) - 1][++m];
-    sOrder[pos] = static_cast<uint16_t>(L);
+    sOrder[pos] = static_cast<uint16_t>(w);
   }
   __syncthreads();
-  if (tid == 0) {
+  if (threadIdx.x == 0) {
     sBadInput = adjacency_ok(sAdj, n) ? 0 : 1;
     if (sBadInput)
       raise_error(p.error, kDevInvalidInput, 0);
@@ -110,21 +149,15 @@ __global__ void __launch_bounds__(TileShape<LB>::kThreads)
   if (sBadInput)
     return;
 
-  const uint8_t* bMin = reinterpret_cast<const uint8_t*>(sMin);
-  const uint8_t* bMax = reinterpret_cast<const uint8_t*>(sMax);
-  const uint8_t* bCnt = reinterpret_cast<const uint8_t*>(sCnt);
-  uint8_t* bT = reinterpret_cast<uint8_t*>(sT);
-  const uint32_t* gT = reinterpret_cast<const uint32_t*>(p.table);
-
   for (;;) {
-    if (tid == 0)
-      sTile = ld_relaxed_s32(p.error) != 0 ? 0xffffffffu : atomicAdd(p.ticket, 1u);
-    __syncthreads();
-    const uint32_t t = sTile;
+    uint32_t t = 0;
+    if (lane == 0)
+      t = ld_relaxed_s32(p.error) != 0 ? 0xffffffffu : atomicAdd(p.ticket, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= lay.ntiles)
       break;
 
-    // Level j and high part H of tile t.
+    // Level j and high part H of tile t (level-major, colex rank inside).
     int j = 0;
     while (lay.level_off[j + 1] <= t)
       ++j;
@@ -142,94 +175,118 @@ __global__ void __launch_bounds__(TileShape<LB>::kThreads)
       }
     }
 
-    // Child tiles H - h, one per thread; wait until each is published.
+    // Lane m < j owns child tile H - (m-th bit of H) and waits for it.
+    uint32_t child = 0;
     bool ok = true;
-    if (tid < j) {
+    if (lane < j) {
       uint32_t rest = H;
-      for (int q = 0; q < tid; ++q)
+      for (int q = 0; q < lane; ++q)
         rest &= rest - 1;
-      const uint32_t hc = H & ~(rest & (0u - rest));
-      const uint32_t child = lay.level_off[j - 1] + lay.rank_high(hc);
-      sChild[tid] = child;
+      child = lay.level_off[j - 1] + lay.rank_high(H & ~(rest & (0u - rest)));
       ok = wait_flag(p.flags + child, p.epoch, p.timeout_ns, p.error);
     }
-    if (__syncthreads_or(!ok))
+    if (__any_sync(0xffffffffu, !ok))
       break;
 
-    // Cross-tile children: whole tiles, 4 subsets per 32-bit word.
-    if (tid < kWords) {
-      uint32_t mn = 0x3F3F3F3Fu, mx = 0u, cnt = 0u;
-      int m = 0;
-      for (; m + 4 <= j; m += 4) {
-        const uint32_t x0 = __ldcg(gT + static_cast<size_t>(sChild[m]) * kWords + tid);
-        const uint32_t x1 = __ldcg(gT + static_cast<size_t>(sChild[m + 1]) * kWords + tid);
-        const uint32_t x2 = __ldcg(gT + static_cast<size_t>(sChild[m + 2]) * kWords + tid);
-        const uint32_t x3 = __ldcg(gT + static_cast<size_t>(sChild[m + 3]) * kWords + tid);
-        const uint32_t y0 = x0 & 0x3F3F3F3Fu, y1 = x1 & 0x3F3F3F3Fu;
-        const uint32_t y2 = x2 & 0x3F3F3F3Fu, y3 = x3 & 0x3F3F3F3Fu;
-        mn = __vminu4(mn, __vminu4(__vminu4(y0, y1), __vminu4(y2, y3)));
-        mx = __vmaxu4(mx, __vmaxu4(__vmaxu4(y0, y1), __vmaxu4(y2, y3)));
-        cnt += ((x0 >> 7) & 0x01010101u) + ((x1 >> 7) & 0x01010101u) +
-               ((x2 >> 7) & 0x01010101u) + ((x3 >> 7) & 0x01010101u);
+    // Cross-tile children: j whole tiles, reduced 4 subsets per word.
+    if constexpr (kWords >= 256) {
+#pragma unroll 1
+      for (int c0 = 0; c0 < kWords; c0 += 256) {
+        uint32_t mn[8], mx[8], ct[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          mn[q] = 0xFFFFFFFFu;
+          mx[q] = 0u;
+          ct[q] = 0u;
+        }
+        int m = 0;
+        for (; m + 2 <= j; m += 2) {
+          const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
+          const uint32_t c_b = __shfl_sync(0xffffffffu, child, m + 1);
+          const uint4* pa = reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane;
+          const uint4* pb = reinterpret_cast<const uint4*>(p.table + (size_t(c_b) << LB)) + (c0 >> 2) + lane;
+          const uint4 a0 = __ldcg(pa), a1 = __ldcg(pa + 32), b0 = __ldcg(pb), b1 = __ldcg(pb + 32);
+          acc_word(a0.x, mn[0], mx[0], ct[0]); acc_word(a0.y, mn[1], mx[1], ct[1]);
+          acc_word(a0.z, mn[2], mx[2], ct[2]); acc_word(a0.w, mn[3], mx[3], ct[3]);
+          acc_word(a1.x, mn[4], mx[4], ct[4]); acc_word(a1.y, mn[5], mx[5], ct[5]);
+          acc_word(a1.z, mn[6], mx[6], ct[6]); acc_word(a1.w, mn[7], mx[7], ct[7]);
+          acc_word(b0.x, mn[0], mx[0], ct[0]); acc_word(b0.y, mn[1], mx[1], ct[1]);
+          acc_word(b0.z, mn[2], mx[2], ct[2]); acc_word(b0.w, mn[3], mx[3], ct[3]);
+          acc_word(b1.x, mn[4], mx[4], ct[4]); acc_word(b1.y, mn[5], mx[5], ct[5]);
+          acc_word(b1.z, mn[6], mx[6], ct[6]); acc_word(b1.w, mn[7], mx[7], ct[7]);
+        }
+        if (m < j) {
+          const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
+          const uint4* pa = reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane;
+          const uint4 a0 = __ldcg(pa), a1 = __ldcg(pa + 32);
+          acc_word(a0.x, mn[0], mx[0], ct[0]); acc_word(a0.y, mn[1], mx[1], ct[1]);
+          acc_word(a0.z, mn[2], mx[2], ct[2]); acc_word(a0.w, mn[3], mx[3], ct[3]);
+          acc_word(a1.x, mn[4], mx[4], ct[4]); acc_word(a1.y, mn[5], mx[5], ct[5]);
+          acc_word(a1.z, mn[6], mx[6], ct[6]); acc_word(a1.w, mn[7], mx[7], ct[7]);
+        }
+        uint4 va, vb, wa, wb;
+        pack_agg(mn[0], mx[0], ct[0], va.x, vb.x); pack_agg(mn[1], mx[1], ct[1], va.y, vb.y);
+        pack_agg(mn[2], mx[2], ct[2], va.z, vb.z); pack_agg(mn[3], mx[3], ct[3], va.w, vb.w);
+        pack_agg(mn[4], mx[4], ct[4], wa.x, wb.x); pack_agg(mn[5], mx[5], ct[5], wa.y, wb.y);
+        pack_agg(mn[6], mx[6], ct[6], wa.z, wb.z); pack_agg(mn[7], mx[7], ct[7], wa.w, wb.w);
+        reinterpret_cast<uint4*>(A + c0)[lane] = va;
+        reinterpret_cast<uint4*>(A + c0)[lane + 32] = wa;
+        reinterpret_cast<uint4*>(B + c0)[lane] = vb;
+        reinterpret_cast<uint4*>(B + c0)[lane + 32] = wb;
       }
-      for (; m < j; ++m) {
-        const uint32_t x = __ldcg(gT + static_cast<size_t>(sChild[m]) * kWords + tid);
-        const uint32_t y = x & 0x3F3F3F3Fu;
-        mn = __vminu4(mn, y);
-        mx = __vmaxu4(mx, y);
-        cnt += (x >> 7) & 0x01010101u;
+    } else {
+      for (int w = lane; w < kWords; w += 32) {
+        uint32_t mn = 0xFFFFFFFFu, mx = 0u, ct = 0u;
+        for (int m = 0; m < j; ++m) {
+          const uint32_t c_a = __shfl_sync(__activemask(), child, m);
+          acc_word(__ldcg(reinterpret_cast<const uint32_t*>(p.table + (size_t(c_a) << LB)) + w), mn, mx, ct);
+        }
+        pack_agg(mn, mx, ct, A[w], B[w]);
       }
-      sMin[tid] = mn;
-      sMax[tid] = mx;
-      sCnt[tid] = cnt;
     }
-    __syncthreads();
+    __syncwarp();
 
-    // In-tile children, resolved in popcount order of the low part.
+    // In-tile children: words in popcount order of the word index, the four
+    // subsets of a word (low bits 00, 01, 10, 11) in popcount order.
     const uint64_t Hfull = static_cast<uint64_t>(H) << LB;
     uint32_t start = 0;
 #pragma unroll 1
-    for (int i = 0; i <= LB; ++i) {
-      const uint32_t count = lay.binom[LB][i];
-      for (uint32_t e = tid; e < count; e += kThreads) {
-        const int L = sOrder[start + e];
-        uint32_t mn = bMin[L], mx = bMax[L], c = bCnt[L];
-        for (uint32_t s = static_cast<uint32_t>(L); s; s &= s - 1) {
-          const uint32_t x = bT[L ^ (s & (0u - s))];
-          mn = min(mn, x & 63u);
-          mx = max(mx, x & 63u);
-          c += x >> 7;
-        }
-        const int k = j + i;
-        uint32_t val;
-        if (k == 0) {
-          val = 0u;
-        } else if (k == 1) {
-          val = 0x81u;
-        } else {
-          bool conn;
-          if (k == 2) {
-            const uint64_t S = Hfull | static_cast<uint64_t>(L);
-            const int u = __ffsll(static_cast<long long>(S)) - 1;
-            const int v = 63 - __clzll(static_cast<long long>(S));
-            conn = (sAdj[u] >> v) & 1ull;
-          } else {
-            conn = c >= 2u;
-          }
-          val = conn ? ((mn + 1u) | 0x80u) : mx;
-        }
-        bT[L] = static_cast<uint8_t>(val);
+    for (int s = 0; s <= kWordBits; ++s) {
+      const uint32_t count = lay.binom[kWordBits][s];
+      for (uint32_t e = lane; e < count; e += 32) {
+        const uint32_t w = sOrder[start + e];
+        const uint32_t a = A[w], b = B[w];
+        uint32_t mn = a & 0x7F7F7F7Fu, mx = b & 0x7F7F7F7Fu;
+        uint32_t ct = ((a >> 7) & 0x01010101u) + ((b >> 7) & 0x01010101u);
+        for (uint32_t r = w; r; r &= r - 1)
+          acc_word(T[w ^ (r & (0u - r))], mn, mx, ct);
+        const int k = j + s;
+        const uint64_t S0 = Hfull | (uint64_t(w) << 2);
+        const uint32_t v0 = resolve(mn & 0xFFu, mx & 0xFFu, ct & 0xFFu, k, S0, sAdj);
+        const uint32_t v1 = resolve(min((mn >> 8) & 0xFFu, v0), max((mx >> 8) & 0xFFu, v0),
+                                    ((ct >> 8) & 0xFFu) + (v0 & 1u), k + 1, S0 | 1u, sAdj);
+        const uint32_t v2 = resolve(min((mn >> 16) & 0xFFu, v0), max((mx >> 16) & 0xFFu, v0),
+                                    ((ct >> 16) & 0xFFu) + (v0 & 1u), k + 1, S0 | 2u, sAdj);
+        const uint32_t v3 = resolve(min(min(mn >> 24, v1), v2), max(max(mx >> 24, v1), v2),
+                                    (ct >> 24) + (v1 & 1u) + (v2 & 1u), k + 2, S0 | 3u, sAdj);
+        T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
       }
       start += count;
-      __syncthreads();
+      __syncwarp();
     }
 
     // Store the tile, then publish it.
-    if (tid < kWords)
-      reinterpret_cast<uint32_t*>(p.table)[static_cast<size_t>(t) * kWords + tid] = sT[tid];
+    uint32_t* dst = reinterpret_cast<uint32_t*>(p.table + (size_t(t) << LB));
+    if constexpr (kWords >= 128) {
+      for (int w4 = lane; w4 < kWords / 4; w4 += 32)
+        reinterpret_cast<uint4*>(dst)[w4] = reinterpret_cast<const uint4*>(T)[w4];
+    } else {
+      for (int w = lane; w < kWords; w += 32)
+        dst[w] = T[w];
+    }
     __threadfence();
-    __syncthreads();
-    if (tid == 0)
+    __syncwarp();
+    if (lane == 0)
       st_release_u32(p.flags + t, p.epoch);
   }
 }
@@ -266,7 +323,7 @@ __device__ uint64_t warp_component(uint64_t S, int v, const uint64_t* adj, int n
 }
 
 __device__ __forceinline__ uint32_t td_of(const DpKernelParams& p, uint64_t S) {
-  return p.table[p.lay.index(S)] & 63u;
+  return p.table[p.lay.index(S)] >> 1;
 }
 
 // First vertex v of the connected set C with td(C - v) = td(C) - 1.
@@ -384,19 +441,25 @@ __global__ void __launch_bounds__(32)
 
 template <int LB>
 static cudaError_t launch_tiles(const DpKernelParams& p, int ctas, cudaStream_t s) {
-  dp_tile_kernel<LB><<<ctas, TileShape<LB>::kThreads, 0, s>>>(p);
+  dp_tile_kernel<LB><<<ctas, 32 * kDpWarps, TileShape<LB>::kSmem, s>>>(p);
   return cudaGetLastError();
 }
 
 template <int LB>
 static int occupancy_tiles() {
+  if (cudaFuncSetAttribute(dp_tile_kernel<LB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(TileShape<LB>::kSmem)) != cudaSuccess)
+    return 0;
   int blocks = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, dp_tile_kernel<LB>,
-                                                TileShape<LB>::kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, dp_tile_kernel<LB>, 32 * kDpWarps,
+                                                TileShape<LB>::kSmem);
   return blocks;
 }
 
-int dp_tile_threads(int lb) { return lb <= 7 ? 32 : (1 << (lb - 2)); }
+int dp_tile_threads(int lb) {
+  (void)lb;
+  return 32 * kDpWarps;
+}
 
 int dp_tile_occupancy(int lb) {
   switch (lb) {

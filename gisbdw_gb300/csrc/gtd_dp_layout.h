@@ -1,7 +1,7 @@
 // Layout of the subset-DP table in device memory (host and device code).
 //
-// Every subset S of the n vertices owns one byte: bits 0-5 hold td(G[S]) and
-// bit 7 is set iff G[S] is connected. Vertices 0..lb-1 are the tile's "low"
+// Every subset S of the n vertices owns one byte, td(G[S]) << 1 | c, where
+// c = 1 iff G[S] is connected. Vertices 0..lb-1 are the tile's "low"
 // vertices and vertices lb..n-1 its "high" ones (nh = n - lb of them). The
 // 2^lb subsets that share the same high part H form one tile of 2^lb
 // contiguous bytes, indexed inside the tile by the low part's bit mask.

@@ -100,7 +100,8 @@ gtd_status gtd_dp_query(gtd_handle h, uint64_t subset_mask, int32_t* td_out,
 
 /* Device pointer and size of the last solve's table (for inspection in
  * tests): entry of subset S lives at gtd_dp_table_index(n, tile_bits, S).
- * Each byte holds td in bits 0-5 and a "connected" flag in bit 7. */
+ * Each byte holds td << 1 | connected (td in bits 1-6, bit 0 set iff the
+ * induced subgraph is connected). */
 gtd_status gtd_dp_table(gtd_handle h, const uint8_t** d_table, uint64_t* bytes,
                         int* n, int* tile_bits);
 uint64_t gtd_dp_table_index(int n, int tile_bits, uint64_t subset_mask);
