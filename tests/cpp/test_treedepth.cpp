@@ -1,0 +1,44 @@
+// C++ drop-in check: the reference's calling pattern (main.cpp:187-195) with
+// a Boost-style adjacency_list (the Boost-API shim from oracle/shim) through
+// include/gtd/treedepth.hpp. Prints "td root order..." per graph; the pytest
+// driver compares with the oracle. Exit code 0 on success.
+#include <boost/graph/adjacency_list.hpp>
+#include <cstdio>
+#include <stdexcept>
+
+#include "gtd/treedepth.hpp"
+
+using Graph = boost::adjacency_list<boost::mapS, boost::vecS, boost::undirectedS>;
+
+int main() {
+  // P7 (elimination_tree_unittest.cpp:188-270): td 3
+  Graph p7(7);
+  for (int i = 0; i < 6; ++i)
+    boost::add_edge(i, i + 1, p7);
+  // C5: td 4
+  Graph c5(5);
+  for (int i = 0; i < 5; ++i)
+    boost::add_edge(i, (i + 1) % 5, c5);
+  td::DynamicGPU dyngpu;
+  for (Graph* g : {&p7, &c5}) {
+    dyngpu(*g);
+    auto el = dyngpu.GetElimination<std::size_t>(boost::num_vertices(*g), boost::num_vertices(*g), 0);
+    auto r = dyngpu.Decompose();
+    std::printf("%u %zu", r.treedepth, r.root);
+    for (auto v : el)
+      std::printf(" %zu", v);
+    std::printf("\n");
+  }
+  // a self loop is rejected with std::invalid_argument, as the reference does
+  Graph bad(3);
+  boost::add_edge(0, 1, bad);
+  boost::add_edge(1, 1, bad);
+  try {
+    dyngpu(bad);
+    std::printf("no-throw\n");
+    return 1;
+  } catch (std::invalid_argument const&) {
+    std::printf("invalid_argument\n");
+  }
+  return 0;
+}
