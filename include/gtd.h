@@ -110,6 +110,31 @@ uint64_t gtd_dp_table_index(int n, int tile_bits, uint64_t subset_mask);
  * memory `out` of `bytes` bytes. */
 gtd_status gtd_dp_read_table(gtd_handle h, uint8_t* out, uint64_t bytes);
 
+/* Largest n gtd_dp_solve_noalloc accepts (its fixed scratch holds a 2^n-byte
+ * table: 16 MiB at n = 24). */
+#define GTD_DP_NOALLOC_MAX_N 24
+
+/* The subset DP for callers that cannot allocate device memory (code running
+ * where cudaMalloc is not allowed, under a pool that must not grow, or next to
+ * a framework that owns all device memory). This entry point has no
+ * counterpart in the reference. It allocates nothing: no handle, no
+ * cudaMalloc/cudaFree. Its scratch is one fixed __device__ array of about
+ * 16.3 MiB that every GPU loading this library holds until process exit, so
+ * it accepts 2 <= n <= GTD_DP_NOALLOC_MAX_N and rejects larger n with
+ * GTD_INVALID_ARG. Inputs and outputs are DEVICE pointers owned by the
+ * caller: adjacency d_adj[n]; outputs d_td (1 int), d_parent[n] and, if
+ * non-null, d_order[n], with the same values as gtd_dp_solve. Runs on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) on the
+ * current device and returns after synchronising that stream. The first
+ * call on each device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. All calls share the one array and it keeps the
+ * previous call's contents (the call clears what must start at zero): calls
+ * whose GPU work overlaps, from two streams or two host threads, race. */
+gtd_status gtd_dp_solve_noalloc(const uint64_t* d_adj, int n, int32_t* d_td,
+                                int32_t* d_parent, int32_t* d_order,
+                                void* stream);
+
 #ifdef __cplusplus
 }
 #endif
