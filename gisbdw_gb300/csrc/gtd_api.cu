@@ -87,10 +87,9 @@ gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info) {
   }
 }
 
-int default_tile_bits(int n) {
-  (void)n;
-  return 10;
-}
+// Tile bits measured best on GB300 (1 KB tiles up to n = 25, 2 KB above:
+// n = 30 3.51 ms with 11 bits vs 3.76 ms with 10 and 4.72 ms with 12).
+int default_tile_bits(int n) { return n >= 26 ? 11 : 10; }
 
 // Allocates (or grows) the table and flag buffers and enqueues the DP and
 // tree kernels. Outputs go to td/parent/order (device pointers, may be the

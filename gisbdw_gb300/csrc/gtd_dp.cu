@@ -52,9 +52,12 @@ struct TileShape {
   static constexpr int kEntries = 1 << LB;
   static constexpr int kWords = kEntries / 4;   // 4 subsets per 32-bit word
   static constexpr int kWordBits = LB - 2;
-  // dynamic shared memory: per warp T, A, B (kWords words each), then the
-  // shared word order (kWords uint16) and the adjacency (kDpMaxN uint64).
-  static constexpr size_t kSmem = size_t(kDpWarps) * 3 * kWords * 4 + kWords * 2 + 16 + kDpMaxN * 8;
+  // dynamic shared memory: per warp T, MN, MX, CT (kWords words each), then
+  // the shared word order (kWords uint16) and the adjacency (kDpMaxN uint64).
+  static constexpr size_t kPerWarp = size_t(4) * kWords * 4;
+  static constexpr size_t kOrderOff = size_t(kDpWarps) * kPerWarp;
+  static constexpr size_t kAdjOff = (kOrderOff + kWords * 2 + 15) & ~size_t(15);
+  static constexpr size_t kSmem = kAdjOff + kDpMaxN * 8;
 };
 
 // Checks the adjacency masks: no self loop, no bit >= n, symmetric.
@@ -75,10 +78,46 @@ __device__ __forceinline__ bool adjacency_ok(const uint64_t* adj, int n) {
   return true;
 }
 
-// Table bytes hold td << 1 | connected, so an unsigned byte min (max) over
+// Table bytes hold td << 1 | connected, so an unsigned min (max) over
 // children gives 2 * min td (2 * max td) plus a flag bit, without masking.
-// Value of one subset from the min/max raw child bytes m, M, the number c of
-// connected children and k = |S|; s2 is S itself (used only when k == 2).
+// Byte-wise SIMD (__vminu4) is emulated on this GPU, so words are split into
+// two 16x2 halves (bytes 0,2 and bytes 1,3) and reduced with the 16-bit
+// two-lane min/max, which are native.
+__device__ __forceinline__ uint32_t lo16(uint32_t x) { return __byte_perm(x, 0u, 0x4240u); }
+__device__ __forceinline__ uint32_t hi16(uint32_t x) { return __byte_perm(x, 0u, 0x4341u); }
+// bytes (l.lane0, h.lane0, l.lane1, h.lane1) back into one word
+__device__ __forceinline__ uint32_t pack16(uint32_t l, uint32_t h) { return __byte_perm(l, h, 0x6240u); }
+
+struct Agg {
+  uint32_t mnl, mnh, mxl, mxh, ct;  // min/max of bytes (0,2) and (1,3); connected-child counts (bytes)
+};
+
+__device__ __forceinline__ void agg_init(Agg& a) {
+  a.mnl = a.mnh = 0xFFFFFFFFu;
+  a.mxl = a.mxh = 0u;
+  a.ct = 0u;
+}
+
+__device__ __forceinline__ void agg_add2(Agg& a, uint32_t x, uint32_t y) {
+  const uint32_t xl = lo16(x), xh = hi16(x), yl = lo16(y), yh = hi16(y);
+  a.mnl = __vimin3_u16x2(a.mnl, xl, yl);
+  a.mnh = __vimin3_u16x2(a.mnh, xh, yh);
+  a.mxl = __vimax3_u16x2(a.mxl, xl, yl);
+  a.mxh = __vimax3_u16x2(a.mxh, xh, yh);
+  a.ct += (x & 0x01010101u) + (y & 0x01010101u);
+}
+
+__device__ __forceinline__ void agg_add1(Agg& a, uint32_t x) {
+  const uint32_t xl = lo16(x), xh = hi16(x);
+  a.mnl = __vminu2(a.mnl, xl);
+  a.mnh = __vminu2(a.mnh, xh);
+  a.mxl = __vmaxu2(a.mxl, xl);
+  a.mxh = __vmaxu2(a.mxh, xh);
+  a.ct += x & 0x01010101u;
+}
+
+// Scalar value of one subset from the min/max raw child bytes m, M, the
+// number c of connected children and k = |S|; s2 is S (used when k == 2).
 __device__ __forceinline__ uint32_t resolve(uint32_t m, uint32_t M, uint32_t c, int k, uint64_t s2,
                                             const uint64_t* adj) {
   if (k <= 1)
@@ -94,17 +133,12 @@ __device__ __forceinline__ uint32_t resolve(uint32_t m, uint32_t M, uint32_t c, 
   return conn ? ((m & ~1u) + 3u) : (M & ~1u);
 }
 
-__device__ __forceinline__ void acc_word(uint32_t x, uint32_t& mn, uint32_t& mx, uint32_t& ct) {
-  mn = __vminu4(mn, x);
-  mx = __vmaxu4(mx, x);
-  ct += x & 0x01010101u;
-}
-
-// Packs the cross-tile aggregates of one word: A = min raw | 0x80 where
-// >= 1 connected child, B = max raw | 0x80 where >= 2 connected children.
-__device__ __forceinline__ void pack_agg(uint32_t mn, uint32_t mx, uint32_t ct, uint32_t& a, uint32_t& b) {
-  a = (mn & 0x7F7F7F7Fu) | (__vcmpgtu4(ct, 0u) & 0x80808080u);
-  b = (mx & 0x7F7F7F7Fu) | (__vcmpgtu4(ct, 0x01010101u) & 0x80808080u);
+// Two subsets at once (16-bit lanes, values in the low byte), |S| >= 3:
+// connected (>= 2 connected children) -> 2 (min td + 1) + 1, else 2 max td.
+__device__ __forceinline__ uint32_t resolve2(uint32_t mn, uint32_t mx, uint32_t ct) {
+  const uint32_t h = (ct + 0x7FFE7FFEu) & 0x80008000u;  // bit 15: count >= 2
+  const uint32_t m = h - (h >> 15);
+  return (((mn & 0xFFFEFFFEu) + 0x00030003u) & m) | (mx & 0xFFFEFFFEu & ~m);
 }
 
 template <int LB>
@@ -117,11 +151,12 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  uint32_t* T = reinterpret_cast<uint32_t*>(smem) + size_t(warp) * 3 * kWords;
-  uint32_t* A = T + kWords;
-  uint32_t* B = A + kWords;
-  uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + size_t(kDpWarps) * 3 * kWords * 4);
-  uint64_t* sAdj = reinterpret_cast<uint64_t*>(smem + ((size_t(kDpWarps) * 3 * kWords * 4 + kWords * 2 + 15) & ~size_t(15)));
+  uint32_t* T = reinterpret_cast<uint32_t*>(smem + size_t(warp) * Shape::kPerWarp);
+  uint32_t* MN = T + kWords;
+  uint32_t* MX = MN + kWords;
+  uint32_t* CT = MX + kWords;
+  uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + Shape::kOrderOff);
+  uint64_t* sAdj = reinterpret_cast<uint64_t*>(smem + Shape::kAdjOff);
   __shared__ int sBadInput;
 
   const DpLayout& lay = p.lay;
@@ -188,66 +223,59 @@ __global__ void __launch_bounds__(32 * kDpWarps)
     if (__any_sync(0xffffffffu, !ok))
       break;
 
-    // Cross-tile children: j whole tiles, reduced 4 subsets per word.
-    if constexpr (kWords >= 256) {
+    // Cross-tile children: j whole tiles, 4 subsets per word, children two
+    // at a time through the 3-way 16-bit min/max.
+    if constexpr (kWords >= 128) {
 #pragma unroll 1
-      for (int c0 = 0; c0 < kWords; c0 += 256) {
-        uint32_t mn[8], mx[8], ct[8];
+      for (int c0 = 0; c0 < kWords; c0 += 128) {
+        Agg g[4];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          mn[q] = 0xFFFFFFFFu;
-          mx[q] = 0u;
-          ct[q] = 0u;
-        }
+        for (int q = 0; q < 4; ++q)
+          agg_init(g[q]);
         int m = 0;
         for (; m + 2 <= j; m += 2) {
           const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
           const uint32_t c_b = __shfl_sync(0xffffffffu, child, m + 1);
-          const uint4* pa = reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane;
-          const uint4* pb = reinterpret_cast<const uint4*>(p.table + (size_t(c_b) << LB)) + (c0 >> 2) + lane;
-          const uint4 a0 = __ldcg(pa), a1 = __ldcg(pa + 32), b0 = __ldcg(pb), b1 = __ldcg(pb + 32);
-          acc_word(a0.x, mn[0], mx[0], ct[0]); acc_word(a0.y, mn[1], mx[1], ct[1]);
-          acc_word(a0.z, mn[2], mx[2], ct[2]); acc_word(a0.w, mn[3], mx[3], ct[3]);
-          acc_word(a1.x, mn[4], mx[4], ct[4]); acc_word(a1.y, mn[5], mx[5], ct[5]);
-          acc_word(a1.z, mn[6], mx[6], ct[6]); acc_word(a1.w, mn[7], mx[7], ct[7]);
-          acc_word(b0.x, mn[0], mx[0], ct[0]); acc_word(b0.y, mn[1], mx[1], ct[1]);
-          acc_word(b0.z, mn[2], mx[2], ct[2]); acc_word(b0.w, mn[3], mx[3], ct[3]);
-          acc_word(b1.x, mn[4], mx[4], ct[4]); acc_word(b1.y, mn[5], mx[5], ct[5]);
-          acc_word(b1.z, mn[6], mx[6], ct[6]); acc_word(b1.w, mn[7], mx[7], ct[7]);
+          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
+          const uint4 b = __ldcg(reinterpret_cast<const uint4*>(p.table + (size_t(c_b) << LB)) + (c0 >> 2) + lane);
+          agg_add2(g[0], a.x, b.x);
+          agg_add2(g[1], a.y, b.y);
+          agg_add2(g[2], a.z, b.z);
+          agg_add2(g[3], a.w, b.w);
         }
         if (m < j) {
           const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
-          const uint4* pa = reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane;
-          const uint4 a0 = __ldcg(pa), a1 = __ldcg(pa + 32);
-          acc_word(a0.x, mn[0], mx[0], ct[0]); acc_word(a0.y, mn[1], mx[1], ct[1]);
-          acc_word(a0.z, mn[2], mx[2], ct[2]); acc_word(a0.w, mn[3], mx[3], ct[3]);
-          acc_word(a1.x, mn[4], mx[4], ct[4]); acc_word(a1.y, mn[5], mx[5], ct[5]);
-          acc_word(a1.z, mn[6], mx[6], ct[6]); acc_word(a1.w, mn[7], mx[7], ct[7]);
+          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
+          agg_add1(g[0], a.x);
+          agg_add1(g[1], a.y);
+          agg_add1(g[2], a.z);
+          agg_add1(g[3], a.w);
         }
-        uint4 va, vb, wa, wb;
-        pack_agg(mn[0], mx[0], ct[0], va.x, vb.x); pack_agg(mn[1], mx[1], ct[1], va.y, vb.y);
-        pack_agg(mn[2], mx[2], ct[2], va.z, vb.z); pack_agg(mn[3], mx[3], ct[3], va.w, vb.w);
-        pack_agg(mn[4], mx[4], ct[4], wa.x, wb.x); pack_agg(mn[5], mx[5], ct[5], wa.y, wb.y);
-        pack_agg(mn[6], mx[6], ct[6], wa.z, wb.z); pack_agg(mn[7], mx[7], ct[7], wa.w, wb.w);
-        reinterpret_cast<uint4*>(A + c0)[lane] = va;
-        reinterpret_cast<uint4*>(A + c0)[lane + 32] = wa;
-        reinterpret_cast<uint4*>(B + c0)[lane] = vb;
-        reinterpret_cast<uint4*>(B + c0)[lane + 32] = wb;
+        reinterpret_cast<uint4*>(MN + c0)[lane] =
+            make_uint4(pack16(g[0].mnl, g[0].mnh), pack16(g[1].mnl, g[1].mnh), pack16(g[2].mnl, g[2].mnh),
+                       pack16(g[3].mnl, g[3].mnh));
+        reinterpret_cast<uint4*>(MX + c0)[lane] =
+            make_uint4(pack16(g[0].mxl, g[0].mxh), pack16(g[1].mxl, g[1].mxh), pack16(g[2].mxl, g[2].mxh),
+                       pack16(g[3].mxl, g[3].mxh));
+        reinterpret_cast<uint4*>(CT + c0)[lane] = make_uint4(g[0].ct, g[1].ct, g[2].ct, g[3].ct);
       }
     } else {
       for (int w = lane; w < kWords; w += 32) {
-        uint32_t mn = 0xFFFFFFFFu, mx = 0u, ct = 0u;
+        Agg g;
+        agg_init(g);
         for (int m = 0; m < j; ++m) {
           const uint32_t c_a = __shfl_sync(__activemask(), child, m);
-          acc_word(__ldcg(reinterpret_cast<const uint32_t*>(p.table + (size_t(c_a) << LB)) + w), mn, mx, ct);
+          agg_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(p.table + (size_t(c_a) << LB)) + w));
         }
-        pack_agg(mn, mx, ct, A[w], B[w]);
+        MN[w] = pack16(g.mnl, g.mnh);
+        MX[w] = pack16(g.mxl, g.mxh);
+        CT[w] = g.ct;
       }
     }
     __syncwarp();
 
-    // In-tile children: words in popcount order of the word index, the four
-    // subsets of a word (low bits 00, 01, 10, 11) in popcount order.
+    // In-tile children: words in popcount order of the word index; inside a
+    // word the subsets with low bits 00, then 01 and 10, then 11.
     const uint64_t Hfull = static_cast<uint64_t>(H) << LB;
     uint32_t start = 0;
 #pragma unroll 1
@@ -255,21 +283,49 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       const uint32_t count = lay.binom[kWordBits][s];
       for (uint32_t e = lane; e < count; e += 32) {
         const uint32_t w = sOrder[start + e];
-        const uint32_t a = A[w], b = B[w];
-        uint32_t mn = a & 0x7F7F7F7Fu, mx = b & 0x7F7F7F7Fu;
-        uint32_t ct = ((a >> 7) & 0x01010101u) + ((b >> 7) & 0x01010101u);
-        for (uint32_t r = w; r; r &= r - 1)
-          acc_word(T[w ^ (r & (0u - r))], mn, mx, ct);
+        const uint32_t mnp = MN[w], mxp = MX[w];
+        Agg g;
+        g.mnl = lo16(mnp);
+        g.mnh = hi16(mnp);
+        g.mxl = lo16(mxp);
+        g.mxh = hi16(mxp);
+        g.ct = CT[w];
+        uint32_t r = w;
+        for (; __popc(r) >= 2; r &= r - 1, r &= r - 1) {
+          const uint32_t b1 = r & (0u - r);
+          const uint32_t r2 = r & (r - 1);
+          agg_add2(g, T[w ^ b1], T[w ^ (r2 & (0u - r2))]);
+        }
+        if (r)
+          agg_add1(g, T[w ^ r]);
         const int k = j + s;
-        const uint64_t S0 = Hfull | (uint64_t(w) << 2);
-        const uint32_t v0 = resolve(mn & 0xFFu, mx & 0xFFu, ct & 0xFFu, k, S0, sAdj);
-        const uint32_t v1 = resolve(min((mn >> 8) & 0xFFu, v0), max((mx >> 8) & 0xFFu, v0),
-                                    ((ct >> 8) & 0xFFu) + (v0 & 1u), k + 1, S0 | 1u, sAdj);
-        const uint32_t v2 = resolve(min((mn >> 16) & 0xFFu, v0), max((mx >> 16) & 0xFFu, v0),
-                                    ((ct >> 16) & 0xFFu) + (v0 & 1u), k + 1, S0 | 2u, sAdj);
-        const uint32_t v3 = resolve(min(min(mn >> 24, v1), v2), max(max(mx >> 24, v1), v2),
-                                    (ct >> 24) + (v1 & 1u) + (v2 & 1u), k + 2, S0 | 3u, sAdj);
-        T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
+        if (k >= 3) {
+          const uint32_t ctl = lo16(g.ct), cth = hi16(g.ct);
+          // subset 00 (byte 0, lane 0 of the low half) is final first
+          uint32_t vl = resolve2(g.mnl, g.mxl, ctl);
+          const uint32_t b0 = vl & 0xFFu, f0 = b0 & 1u;
+          // fold it into subsets 10 (low half lane 1) and 01 (high half lane 0)
+          vl = resolve2(__vminu2(g.mnl, (b0 << 16) | 0xFFFFu), __vmaxu2(g.mxl, b0 << 16), ctl + (f0 << 16));
+          const uint32_t mnh = __vminu2(g.mnh, b0 | 0xFFFF0000u), mxh = __vmaxu2(g.mxh, b0);
+          uint32_t vh = resolve2(mnh, mxh, cth + f0);
+          // fold subsets 01 and 10 into 11 (high half lane 1)
+          const uint32_t b1 = vh & 0xFFu, b2 = vl >> 16;
+          vh = resolve2(__vminu2(mnh, (min(b1, b2) << 16) | 0xFFFFu), __vmaxu2(mxh, max(b1, b2) << 16),
+                        cth + f0 + (((b1 & 1u) + (b2 & 1u)) << 16));
+          T[w] = pack16(vl, vh);
+        } else {
+          // small subsets (|S| <= 2 possible): one byte at a time
+          const uint32_t mn = pack16(g.mnl, g.mnh), mx = pack16(g.mxl, g.mxh), ct = g.ct;
+          const uint64_t S0 = Hfull | (uint64_t(w) << 2);
+          const uint32_t v0 = resolve(mn & 0xFFu, mx & 0xFFu, ct & 0xFFu, k, S0, sAdj);
+          const uint32_t v1 = resolve(min((mn >> 8) & 0xFFu, v0), max((mx >> 8) & 0xFFu, v0),
+                                      ((ct >> 8) & 0xFFu) + (v0 & 1u), k + 1, S0 | 1u, sAdj);
+          const uint32_t v2 = resolve(min((mn >> 16) & 0xFFu, v0), max((mx >> 16) & 0xFFu, v0),
+                                      ((ct >> 16) & 0xFFu) + (v0 & 1u), k + 1, S0 | 2u, sAdj);
+          const uint32_t v3 = resolve(min(min(mn >> 24, v1), v2), max(max(mx >> 24, v1), v2),
+                                      (ct >> 24) + (v1 & 1u) + (v2 & 1u), k + 2, S0 | 3u, sAdj);
+          T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
+        }
       }
       start += count;
       __syncwarp();
