@@ -67,6 +67,25 @@ class DpStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class GraphDesc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("offset", ctypes.c_int32)]
+
+
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("tile_bits", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("timeout_ns", ctypes.c_uint64), ("use_cuda_graph", ctypes.c_int)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("dp_ms", ctypes.c_float), ("total_ms", ctypes.c_float),
+                ("subsets", ctypes.c_uint64), ("alg_bytes", ctypes.c_uint64),
+                ("table_bytes", ctypes.c_uint64), ("tile_bits", ctypes.c_int),
+                ("tiles", ctypes.c_int), ("ctas", ctypes.c_int), ("graph_replayed", ctypes.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _LIB = None
 _LOCK = threading.Lock()
 
@@ -100,8 +119,13 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                    ctypes.POINTER(_i), ctypes.POINTER(_i)]
         L.gtd_dp_table_index.restype = _u64
         L.gtd_dp_table_index.argtypes = [_i, _i, _u64]
-        if hasattr(L, "gtd_dp_read_table"):
-            L.gtd_dp_read_table.argtypes = [_vp, _vp, _u64]
+        L.gtd_dp_read_table.argtypes = [_vp, _vp, _u64]
+        L.gtd_dp_solve_batch.argtypes = [_vp, _vp, _i, _vp, ctypes.c_int64, _vp, _vp,
+                                         ctypes.POINTER(BatchOpts), ctypes.POINTER(BatchStats)]
+        L.gtd_dp_solve_batch_device.argtypes = [_vp, _vp, _i, _vp, ctypes.c_int64, _vp, _vp,
+                                                ctypes.POINTER(BatchOpts)]
+        L.gtd_dp_batch_sync.argtypes = [_vp, ctypes.POINTER(BatchStats)]
+        L.gtd_dp_autotune.argtypes = [_vp, _i, _i, _vp]
         _LIB = L
         return L
 
@@ -177,6 +201,39 @@ class Handle:
                                         _ptr(order) if want_order else None))
         return td.value, (order[:k].tolist() if want_order else None)
 
+    # -- batched subset DP -------------------------------------------------
+    def dp_solve_batch(self, graphs, tile_bits: int = 0, ctas_per_sm: int = 0, timeout_ns: int = 0,
+                       use_cuda_graph: bool = True, packed=None):
+        """Solves every graph; returns (td[count], [parent arrays], stats)."""
+        descs, pool = packed if packed is not None else pack_batch(graphs)
+        count = len(descs)
+        td = np.zeros(count, dtype=np.int32)
+        parent = np.zeros(max(1, pool.size), dtype=np.int32)
+        opts = BatchOpts(tile_bits, ctas_per_sm, timeout_ns, int(use_cuda_graph))
+        stats = BatchStats()
+        self._check(self.L.gtd_dp_solve_batch(self._h, ctypes.cast(descs, _vp), count, _ptr(pool), pool.size,
+                                              _ptr(td), _ptr(parent), ctypes.byref(opts), ctypes.byref(stats)))
+        parents = [parent[d.offset:d.offset + d.n] for d in descs]
+        return td, parents, stats.as_dict()
+
+    def dp_solve_batch_device(self, descs, count: int, d_pool: int, pool_len: int, d_td: int, d_parent: int,
+                              tile_bits: int = 0, ctas_per_sm: int = 0, timeout_ns: int = 0,
+                              use_cuda_graph: bool = True) -> None:
+        opts = BatchOpts(tile_bits, ctas_per_sm, timeout_ns, int(use_cuda_graph))
+        self._check(self.L.gtd_dp_solve_batch_device(self._h, ctypes.cast(descs, _vp), count, _vp(d_pool),
+                                                     pool_len, _vp(d_td), _vp(d_parent), ctypes.byref(opts)))
+
+    def dp_batch_sync(self) -> dict:
+        stats = BatchStats()
+        self._check(self.L.gtd_dp_batch_sync(self._h, ctypes.byref(stats)))
+        return stats.as_dict()
+
+    def dp_autotune(self, n_min: int, n_max: int) -> np.ndarray:
+        """Rates (subsets per microsecond), rows n_min..n_max, columns tile bits 8..12."""
+        rates = np.zeros((n_max - n_min + 1, 5), dtype=np.float32)
+        self._check(self.L.gtd_dp_autotune(self._h, n_min, n_max, _ptr(rates)))
+        return rates
+
     def dp_table_info(self) -> Tuple[int, int, int, int]:
         ptr, nbytes, n, lb = _vp(), _u64(), _i(), _i()
         self._check(self.L.gtd_dp_table(self._h, ctypes.byref(ptr), ctypes.byref(nbytes),
@@ -189,6 +246,20 @@ class Handle:
         out = np.empty(nbytes, dtype=np.uint8)
         self._check(self.L.gtd_dp_read_table(self._h, _ptr(out), nbytes))
         return out, n, lb
+
+
+def pack_batch(graphs):
+    """Adjacency pool and descriptors for a list of graphs (offsets = running
+    sum of n)."""
+    descs = (GraphDesc * len(graphs))()
+    off = 0
+    pool = np.zeros(sum(g.n for g in graphs), dtype=np.uint64)
+    for i, g in enumerate(graphs):
+        descs[i].n = g.n
+        descs[i].offset = off
+        pool[off:off + g.n] = g.adj64()
+        off += g.n
+    return descs, pool
 
 
 def table_index(n: int, tile_bits: int, subset_mask: int) -> int:

@@ -1,6 +1,6 @@
-// C ABI of the gtd library: handles and the subset-DP entry points.
-// Errors never cross the ABI as exceptions; every call returns gtd_status and
-// keeps a message for gtd_last_error.
+// C ABI of the gtd library: handles and the single-graph subset-DP entry
+// points. Errors never cross the ABI as exceptions; every call returns a
+// gtd_status and keeps a message for gtd_last_error.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -9,7 +9,6 @@
 #include <new>
 #include <string>
 
-#include "gtd_device.cuh"
 #include "gtd_handle.h"
 
 namespace gtd {
@@ -24,32 +23,6 @@ gtd_status cuda_fail(gtd_handle h, cudaError_t e, const char* what) {
   std::string m = std::string(what) + ": " + cudaGetErrorString(e);
   return fail(h, e == cudaErrorMemoryAllocation ? GTD_OOM : GTD_CUDA_ERROR, m);
 }
-
-namespace {
-
-// Makes the handle's device current for the duration of a call and restores
-// the caller's device afterwards.
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess)
-      prev = -1;
-    if (prev != dev)
-      cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
-      cudaSetDevice(prev);
-  }
-};
-
-#define GTD_CUDA(h, call)                         \
-  do {                                            \
-    cudaError_t e_ = (call);                      \
-    if (e_ != cudaSuccess)                        \
-      return ::gtd::cuda_fail((h), e_, #call);    \
-  } while (0)
 
 gtd_status check_adjacency(gtd_handle h, const uint64_t* adj, int n) {
   const uint64_t allowed = n >= 64 ? ~0ull : ((1ull << n) - 1);
@@ -73,11 +46,13 @@ gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info) {
     case kDevOk:
       return GTD_OK;
     case kDevInvalidInput:
-      return fail(h, GTD_INVALID_ARG, "adjacency rejected on the device (self loop, bit >= n or asymmetric)");
+      return fail(h, GTD_INVALID_ARG,
+                  "adjacency rejected on the device (self loop, bit >= n or asymmetric; graph " +
+                      std::to_string(info) + ")");
     case kDevWaitTimeout:
       return fail(h, GTD_TIMEOUT, "a tile dependency wait exceeded its deadline");
     case kDevNoRoot:
-      return fail(h, GTD_ABORTED, "tree reconstruction found no optimal root (info " + std::to_string(info) + ")");
+      return fail(h, GTD_ABORTED, "tree reconstruction found no optimal root (graph " + std::to_string(info) + ")");
     case kDevDeadline:
       return fail(h, GTD_TIMEOUT, "search deadline reached");
     case kDevOverflow:
@@ -87,65 +62,105 @@ gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info) {
   }
 }
 
+cudaError_t ensure_device(void** ptr, size_t* cap, size_t bytes) {
+  if (*cap >= bytes && *ptr)
+    return cudaSuccess;
+  if (*ptr)
+    cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  const size_t want = bytes < 256 ? 256 : bytes;
+  cudaError_t e = cudaMalloc(ptr, want);
+  if (e == cudaSuccess)
+    *cap = want;
+  return e;
+}
+
+gtd_status ensure_flags(gtd_handle h, size_t tiles) {
+  if (h->flags_cap >= tiles && h->d_flags)
+    return GTD_OK;
+  size_t cap_bytes = h->flags_cap * sizeof(uint32_t);
+  void* p = h->d_flags;
+  GTD_CUDA(h, ensure_device(&p, &cap_bytes, tiles * sizeof(uint32_t)));
+  h->d_flags = static_cast<uint32_t*>(p);
+  h->flags_cap = cap_bytes / sizeof(uint32_t);
+  GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, cap_bytes, h->stream));
+  h->epoch = 0;
+  return GTD_OK;
+}
+
+gtd_status next_epoch(gtd_handle h, uint32_t* epoch) {
+  if (++h->epoch >= kGraphEpoch) {
+    GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, h->flags_cap * sizeof(uint32_t), h->stream));
+    h->epoch = 1;
+  }
+  *epoch = h->epoch;
+  return GTD_OK;
+}
+
+namespace {
+
 // Tile bits measured best on GB300 (1 KB tiles up to n = 25, 2 KB above:
 // n = 30 3.51 ms with 11 bits vs 3.76 ms with 10 and 4.72 ms with 12).
 int default_tile_bits(int n) { return n >= 26 ? 11 : 10; }
 
-// Allocates (or grows) the table and flag buffers and enqueues the DP and
-// tree kernels. Outputs go to td/parent/order (device pointers, may be the
-// handle's IO block).
+// Allocates (or grows) the table and flag buffers and enqueues the
+// validation, DP and tree kernels for one graph. Outputs go to
+// td/parent/order (device pointers, possibly the handle's IO block).
 gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_opts* opts,
                       int32_t* d_td, int32_t* d_parent, int32_t* d_order) {
   const int tile_bits = (opts && opts->tile_bits > 0) ? opts->tile_bits : default_tile_bits(n);
-  DpKernelParams p;
-  p.lay = make_dp_layout(n, tile_bits);
+  const DpLayout L = make_dp_layout(n, tile_bits);
   const size_t table_bytes = size_t(1) << n;
-  if (h->table_cap < table_bytes) {
-    if (h->d_table)
-      cudaFree(h->d_table);
-    h->d_table = nullptr;
-    h->table_cap = 0;
+  if (h->table_cap < table_bytes)
     h->have_table = false;
-    GTD_CUDA(h, cudaMalloc(&h->d_table, table_bytes < 256 ? 256 : table_bytes));
-    h->table_cap = table_bytes < 256 ? 256 : table_bytes;
-  }
-  if (h->flags_cap < p.lay.ntiles) {
-    if (h->d_flags)
-      cudaFree(h->d_flags);
-    h->d_flags = nullptr;
-    h->flags_cap = 0;
-    GTD_CUDA(h, cudaMalloc(&h->d_flags, sizeof(uint32_t) * p.lay.ntiles));
-    GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * p.lay.ntiles, h->stream));
-    h->flags_cap = p.lay.ntiles;
-    h->epoch = 0;
-  }
-  if (++h->epoch == 0xffffffffu) {
-    GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * h->flags_cap, h->stream));
-    h->epoch = 1;
-  }
+  void* tp = h->d_table;
+  GTD_CUDA(h, ensure_device(&tp, &h->table_cap, table_bytes));
+  h->d_table = static_cast<uint8_t*>(tp);
+  gtd_status s = ensure_flags(h, L.ntiles);
+  if (s != GTD_OK)
+    return s;
+
+  DpBatchParams p;
+  dp_fill_binom(p);
+  p.single.table_off = 0;
+  p.single.tile_base = 0;
+  p.single.ntiles = L.ntiles;
+  p.single.adj_off = 0;
+  p.single.n = n;
+  p.single.nh = L.nh;
+  p.single.out_idx = 0;
+  p.num_graphs = 1;
+  p.lb = L.lb;
+  p.total_tiles = L.ntiles;
   p.table = h->d_table;
   p.flags = h->d_flags;
   p.ticket = reinterpret_cast<uint32_t*>(h->d_io + kIoTicket);
   p.error = h->d_io + kIoError;
   p.adj = d_adj;
-  p.epoch = h->epoch;
+  s = next_epoch(h, &p.epoch);
+  if (s != GTD_OK)
+    return s;
   p.timeout_ns = (opts && opts->timeout_ns) ? opts->timeout_ns : 10ull * 1000 * 1000 * 1000;
+  p.td_out = d_td;
+  p.parent_out = d_parent;
+  p.order_out = d_order;
 
-  int occ = dp_tile_occupancy(p.lay.lb);
+  int occ = dp_tile_occupancy(p.lb);
   if (opts && opts->ctas_per_sm > 0 && opts->ctas_per_sm < occ)
     occ = opts->ctas_per_sm;
   if (occ < 1)
     occ = 1;
   long long ctas = static_cast<long long>(h->num_sms) * occ;
-  if (ctas > p.lay.ntiles)
-    ctas = p.lay.ntiles;
+  if (ctas > p.total_tiles)
+    ctas = p.total_tiles;
 
   GTD_CUDA(h, cudaMemsetAsync(h->d_io, 0, 4 * sizeof(int32_t), h->stream));
+  GTD_CUDA(h, dp_launch_validate(p, h->stream));
   GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
   GTD_CUDA(h, dp_launch_tiles(p, static_cast<int>(ctas), h->stream));
   GTD_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
-  const uint64_t full = n == 64 ? ~0ull : ((1ull << n) - 1);
-  GTD_CUDA(h, dp_launch_tree(p, full, d_td, d_parent, d_order, h->stream));
+  GTD_CUDA(h, dp_launch_tree(p, h->stream));
   GTD_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
 
   h->last_params = p;
@@ -155,8 +170,8 @@ gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_o
   st = gtd_dp_stats{};
   st.table_bytes = table_bytes;
   st.alg_bytes = table_bytes + static_cast<uint64_t>(n) * (table_bytes / 2);
-  st.tile_bits = p.lay.lb;
-  st.tiles = static_cast<int>(p.lay.ntiles);
+  st.tile_bits = p.lb;
+  st.tiles = static_cast<int>(p.total_tiles);
   st.ctas = static_cast<int>(ctas);
   return GTD_OK;
 }
@@ -245,12 +260,21 @@ gtd_status gtd_destroy(gtd_handle h) {
     DeviceGuard g(h->device);
     if (h->stream)
       cudaStreamSynchronize(h->stream);
+    if (h->bgraph)
+      cudaGraphExecDestroy(h->bgraph);
     cudaFree(h->d_table);
     cudaFree(h->d_flags);
     cudaFree(h->d_io);
     cudaFree(h->d_adj);
+    cudaFree(h->d_bgraphs);
+    cudaFree(h->d_tile_graph);
+    cudaFree(h->d_badj);
+    cudaFree(h->d_btd);
+    cudaFree(h->d_bparent);
     if (h->h_pinned)
       cudaFreeHost(h->h_pinned);
+    if (h->h_bstage)
+      cudaFreeHost(h->h_bstage);
     for (auto& e : h->ev)
       if (e)
         cudaEventDestroy(e);
@@ -261,9 +285,8 @@ gtd_status gtd_destroy(gtd_handle h) {
   return GTD_OK;
 }
 
-gtd_status gtd_dp_solve(gtd_handle h, const uint64_t* adj, int n, int32_t* td_out,
-                        int32_t* parent_out, int32_t* order_out, const gtd_dp_opts* opts,
-                        gtd_dp_stats* stats) {
+gtd_status gtd_dp_solve(gtd_handle h, const uint64_t* adj, int n, int32_t* td_out, int32_t* parent_out,
+                        int32_t* order_out, const gtd_dp_opts* opts, gtd_dp_stats* stats) {
   if (!h)
     return GTD_INVALID_ARG;
   if (!adj || !td_out || !parent_out)
@@ -312,8 +335,8 @@ gtd_status gtd_dp_solve(gtd_handle h, const uint64_t* adj, int n, int32_t* td_ou
   return GTD_OK;
 }
 
-gtd_status gtd_dp_solve_device(gtd_handle h, const uint64_t* d_adj, int n, int32_t* d_td,
-                               int32_t* d_parent, int32_t* d_order, const gtd_dp_opts* opts) {
+gtd_status gtd_dp_solve_device(gtd_handle h, const uint64_t* d_adj, int n, int32_t* d_td, int32_t* d_parent,
+                               int32_t* d_order, const gtd_dp_opts* opts) {
   if (!h)
     return GTD_INVALID_ARG;
   if (!d_adj || !d_td || !d_parent)
@@ -345,15 +368,23 @@ gtd_status gtd_dp_query(gtd_handle h, uint64_t subset_mask, int32_t* td_out, int
     return GTD_INVALID_ARG;
   if (!h->have_table)
     return fail(h, GTD_NO_RESULT, "no DP table: solve a graph first");
-  const int n = h->last_params.lay.n;
+  const int n = h->last_params.single.n;
   if (n < 64 && (subset_mask >> n))
     return fail(h, GTD_INVALID_ARG, "subset has a vertex >= n");
   if (!td_out)
     return fail(h, GTD_INVALID_ARG, "null td_out");
+  if (subset_mask == 0) {
+    *td_out = 0;
+    return GTD_OK;
+  }
   DeviceGuard g(h->device);
+  DpBatchParams p = h->last_params;
+  p.query = subset_mask;
+  p.td_out = h->d_io + kIoTd;
+  p.parent_out = nullptr;
+  p.order_out = order_out ? h->d_io + kIoOrder : nullptr;
   GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoError, 0, 2 * sizeof(int32_t), h->stream));
-  GTD_CUDA(h, dp_launch_tree(h->last_params, subset_mask, h->d_io + kIoTd, nullptr,
-                             order_out ? h->d_io + kIoOrder : nullptr, h->stream));
+  GTD_CUDA(h, dp_launch_tree(p, h->stream));
   int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
   GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, (kIoOrder + 64) * sizeof(int32_t), cudaMemcpyDeviceToHost,
                               h->stream));
@@ -375,11 +406,11 @@ gtd_status gtd_dp_table(gtd_handle h, const uint8_t** d_table, uint64_t* bytes, 
   if (d_table)
     *d_table = h->d_table;
   if (bytes)
-    *bytes = uint64_t(1) << h->last_params.lay.n;
+    *bytes = uint64_t(1) << h->last_params.single.n;
   if (n)
-    *n = h->last_params.lay.n;
+    *n = h->last_params.single.n;
   if (tile_bits)
-    *tile_bits = h->last_params.lay.lb;
+    *tile_bits = h->last_params.lb;
   return GTD_OK;
 }
 
@@ -388,7 +419,7 @@ gtd_status gtd_dp_read_table(gtd_handle h, uint8_t* out, uint64_t bytes) {
     return GTD_INVALID_ARG;
   if (!h->have_table)
     return fail(h, GTD_NO_RESULT, "no DP table: solve a graph first");
-  const uint64_t need = uint64_t(1) << h->last_params.lay.n;
+  const uint64_t need = uint64_t(1) << h->last_params.single.n;
   if (!out || bytes < need)
     return fail(h, GTD_INVALID_ARG, "output buffer smaller than the table");
   DeviceGuard g(h->device);

@@ -1,0 +1,421 @@
+// Batched subset DP: many graphs of uneven size in one persistent launch.
+//
+// Planning (host): graphs are put in descending n (largest first, so the
+// tail of the launch is made of small graphs), each gets a table region, a
+// tile range in the global ticket order and a descriptor; the tile->graph
+// lookup is filled on the device. The launch sequence (zero the flags and
+// control words, validate, DP, tree) is captured once in a CUDA graph and
+// replayed while the batch keeps its shape and buffers.
+//
+// The autotuner times the DP kernel per (n, tile bits) on seeded random
+// graphs and the planner then picks, for a whole batch, the tile size with
+// the smallest predicted time (sum over graphs of padded subsets / rate).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "gtd_handle.h"
+
+namespace gtd {
+namespace {
+
+struct Plan {
+  int lb = 10;
+  std::vector<DpGraph> graphs;  // processing order
+  uint64_t table_bytes = 0;
+  uint32_t total_tiles = 0;
+  uint64_t subsets = 0;
+  uint64_t alg_bytes = 0;
+};
+
+int pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const gtd_dp_batch_opts* opts) {
+  if (opts && opts->tile_bits > 0)
+    return std::min(std::max(opts->tile_bits, kTuneLbMin), kTuneLbMax);
+  int best = 10;
+  double best_cost = -1;
+  for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb) {
+    double cost = 0;
+    bool known = true;
+    for (int i = 0; i < count && known; ++i) {
+      const float rate = h->tune[descs[i].n][lb];
+      if (rate <= 0)
+        known = false;
+      else
+        cost += double(uint64_t(1) << std::max(descs[i].n, lb)) / rate;
+    }
+    if (known && (best_cost < 0 || cost < best_cost)) {
+      best_cost = cost;
+      best = lb;
+    }
+  }
+  return best;
+}
+
+Plan make_plan(int lb, const gtd_graph_desc* descs, int count) {
+  Plan P;
+  P.lb = lb;
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return descs[a].n > descs[b].n; });
+  P.graphs.resize(count);
+  uint64_t off = 0;
+  uint32_t tile = 0;
+  for (int k = 0; k < count; ++k) {
+    const gtd_graph_desc& d = descs[order[k]];
+    DpGraph& G = P.graphs[k];
+    G.n = d.n;
+    G.nh = d.n > lb ? d.n - lb : 0;
+    G.ntiles = 1u << G.nh;
+    G.table_off = off;
+    G.tile_base = tile;
+    G.adj_off = static_cast<uint32_t>(d.offset);
+    G.out_idx = order[k];
+    off += uint64_t(G.ntiles) << lb;
+    tile += G.ntiles;
+    const uint64_t sub = uint64_t(1) << d.n;
+    P.subsets += sub;
+    P.alg_bytes += sub + uint64_t(d.n) * (sub / 2);
+  }
+  P.table_bytes = off;
+  P.total_tiles = tile;
+  return P;
+}
+
+uint64_t fingerprint(const Plan& P, const void* adj, const void* td, const void* par, int ctas,
+                     uint64_t timeout) {
+  uint64_t x = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) {
+    x ^= v + 0x9e3779b97f4a7c15ull + (x << 6) + (x >> 2);
+  };
+  mix(P.lb);
+  mix(P.graphs.size());
+  for (const DpGraph& G : P.graphs) {
+    mix(G.n);
+    mix(G.adj_off);
+    mix(G.out_idx);
+  }
+  mix(reinterpret_cast<uintptr_t>(adj));
+  mix(reinterpret_cast<uintptr_t>(td));
+  mix(reinterpret_cast<uintptr_t>(par));
+  mix(ctas);
+  mix(timeout);
+  return x;
+}
+
+gtd_status check_descs(gtd_handle h, const gtd_graph_desc* descs, int count, int64_t pool_len) {
+  if (!descs || count < 1)
+    return fail(h, GTD_INVALID_ARG, "empty batch");
+  for (int i = 0; i < count; ++i) {
+    const gtd_graph_desc& d = descs[i];
+    if (d.n < 1 || d.n > GTD_DP_MAX_N)
+      return fail(h, GTD_INVALID_ARG, "graph " + std::to_string(i) + ": n out of range");
+    if (d.offset < 0 || int64_t(d.offset) + d.n > pool_len)
+      return fail(h, GTD_INVALID_ARG, "graph " + std::to_string(i) + ": offset outside the pool");
+  }
+  return GTD_OK;
+}
+
+// Plans the batch, (re)builds device state when the shape changed and
+// enqueues the launch (graph replay or direct). Device pointers in/out.
+gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, const uint64_t* d_adj,
+                         int32_t* d_td, int32_t* d_parent, const gtd_dp_batch_opts* opts) {
+  const int lb = pick_tile_bits(h, descs, count, opts);
+  Plan P = make_plan(lb, descs, count);
+  const uint64_t timeout = (opts && opts->timeout_ns) ? opts->timeout_ns : 10ull * 1000 * 1000 * 1000;
+  int occ = dp_tile_occupancy(lb);
+  if (opts && opts->ctas_per_sm > 0 && opts->ctas_per_sm < occ)
+    occ = opts->ctas_per_sm;
+  if (occ < 1)
+    occ = 1;
+  long long ctas = static_cast<long long>(h->num_sms) * occ;
+  if (ctas > P.total_tiles)
+    ctas = P.total_tiles;
+  const bool use_graph = !opts || opts->use_cuda_graph;
+  const uint64_t key = fingerprint(P, d_adj, d_td, d_parent, static_cast<int>(ctas), timeout);
+
+  gtd_dp_batch_stats& st = h->bstats;
+  st = gtd_dp_batch_stats{};
+  st.subsets = P.subsets;
+  st.alg_bytes = P.alg_bytes;
+  st.table_bytes = P.table_bytes;
+  st.tile_bits = lb;
+  st.tiles = static_cast<int>(P.total_tiles);
+  st.ctas = static_cast<int>(ctas);
+
+  if (use_graph && h->bgraph_valid && h->bgraph_key == key) {
+    st.graph_replayed = 1;
+    GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+    GTD_CUDA(h, cudaGraphLaunch(h->bgraph, h->stream));
+    GTD_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+    h->have_table = false;
+    return GTD_OK;
+  }
+
+  // Device state for this shape.
+  h->have_table = false;
+  h->bgraph_valid = false;
+  void* p = h->d_table;
+  GTD_CUDA(h, ensure_device(&p, &h->table_cap, P.table_bytes));
+  h->d_table = static_cast<uint8_t*>(p);
+  gtd_status s = ensure_flags(h, P.total_tiles);
+  if (s != GTD_OK)
+    return s;
+  p = h->d_tile_graph;
+  size_t cap = h->tile_graph_cap * sizeof(uint32_t);
+  GTD_CUDA(h, ensure_device(&p, &cap, P.total_tiles * sizeof(uint32_t)));
+  h->d_tile_graph = static_cast<uint32_t*>(p);
+  h->tile_graph_cap = cap / sizeof(uint32_t);
+  p = h->d_bgraphs;
+  cap = h->bgraphs_cap * sizeof(DpGraph);
+  GTD_CUDA(h, ensure_device(&p, &cap, count * sizeof(DpGraph)));
+  h->d_bgraphs = static_cast<DpGraph*>(p);
+  h->bgraphs_cap = cap / sizeof(DpGraph);
+  // Descriptors go up through pinned staging (synchronised below, so the
+  // staging can be reused right after).
+  void* stage = nullptr;
+  GTD_CUDA(h, cudaMallocHost(&stage, count * sizeof(DpGraph)));
+  std::memcpy(stage, P.graphs.data(), count * sizeof(DpGraph));
+  cudaError_t e = cudaMemcpyAsync(h->d_bgraphs, stage, count * sizeof(DpGraph), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(h->stream);
+  cudaFreeHost(stage);
+  GTD_CUDA(h, e);
+
+  DpBatchParams& bp = h->bparams;
+  bp = DpBatchParams{};
+  dp_fill_binom(bp);
+  bp.graphs = h->d_bgraphs;
+  bp.tile_graph = h->d_tile_graph;
+  bp.num_graphs = count;
+  bp.lb = lb;
+  bp.total_tiles = P.total_tiles;
+  bp.table = h->d_table;
+  bp.flags = h->d_flags;
+  bp.ticket = reinterpret_cast<uint32_t*>(h->d_io + kIoTicket);
+  bp.error = h->d_io + kIoError;
+  bp.adj = d_adj;
+  bp.timeout_ns = timeout;
+  bp.td_out = d_td;
+  bp.parent_out = d_parent;
+  GTD_CUDA(h, dp_launch_fill_tile_graph(bp, h->stream));
+
+  if (use_graph) {
+    if (h->bgraph) {
+      cudaGraphExecDestroy(h->bgraph);
+      h->bgraph = nullptr;
+    }
+    bp.epoch = kGraphEpoch;
+    cudaGraph_t graph = nullptr;
+    GTD_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaMemsetAsync(h->d_flags, 0, size_t(P.total_tiles) * sizeof(uint32_t), h->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemsetAsync(h->d_io, 0, 4 * sizeof(int32_t), h->stream);
+    if (ce == cudaSuccess)
+      ce = dp_launch_validate(bp, h->stream);
+    if (ce == cudaSuccess)
+      ce = dp_launch_tiles(bp, static_cast<int>(ctas), h->stream);
+    if (ce == cudaSuccess)
+      ce = dp_launch_tree(bp, h->stream);
+    cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
+    if (ce == cudaSuccess)
+      ce = ee;
+    if (ce == cudaSuccess)
+      ce = cudaGraphInstantiate(&h->bgraph, graph, 0);
+    if (graph)
+      cudaGraphDestroy(graph);
+    GTD_CUDA(h, ce);
+    h->bgraph_key = key;
+    h->bgraph_valid = true;
+    GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+    GTD_CUDA(h, cudaGraphLaunch(h->bgraph, h->stream));
+    GTD_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+  } else {
+    s = next_epoch(h, &bp.epoch);
+    if (s != GTD_OK)
+      return s;
+    GTD_CUDA(h, cudaMemsetAsync(h->d_io, 0, 4 * sizeof(int32_t), h->stream));
+    GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+    GTD_CUDA(h, dp_launch_validate(bp, h->stream));
+    GTD_CUDA(h, dp_launch_tiles(bp, static_cast<int>(ctas), h->stream));
+    GTD_CUDA(h, dp_launch_tree(bp, h->stream));
+    GTD_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+  }
+  return GTD_OK;
+}
+
+gtd_status batch_finish(gtd_handle h, gtd_dp_batch_stats* stats) {
+  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
+  GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  GTD_CUDA(h, cudaStreamSynchronize(h->stream));
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]) == cudaSuccess)
+    h->bstats.dp_ms = ms;
+  if (stats)
+    *stats = h->bstats;
+  return map_device_error(h, h_io[kIoError], h_io[kIoError + 1]);
+}
+
+gtd_status grow_pinned(gtd_handle h, size_t bytes) {
+  if (h->bstage_cap >= bytes)
+    return GTD_OK;
+  if (h->h_bstage)
+    cudaFreeHost(h->h_bstage);
+  h->h_bstage = nullptr;
+  h->bstage_cap = 0;
+  GTD_CUDA(h, cudaMallocHost(&h->h_bstage, bytes));
+  h->bstage_cap = bytes;
+  return GTD_OK;
+}
+
+// Seeded random G(n, 0.3) graphs for the autotuner (splitmix64 draws).
+void random_graph(int n, uint64_t seed, uint64_t* adj) {
+  uint64_t s = seed * 0x9E3779B97F4A7C15ull + 0x243F6A8885A308D3ull;
+  for (int v = 0; v < n; ++v)
+    adj[v] = 0;
+  for (int u = 0; u < n; ++u)
+    for (int v = u + 1; v < n; ++v) {
+      s += 0x9E3779B97F4A7C15ull;
+      uint64_t z = s;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      z ^= z >> 31;
+      if ((z >> 11) * (1.0 / 9007199254740992.0) < 0.3) {
+        adj[u] |= 1ull << v;
+        adj[v] |= 1ull << u;
+      }
+    }
+}
+
+}  // namespace
+}  // namespace gtd
+
+using namespace gtd;
+
+extern "C" {
+
+gtd_status gtd_dp_solve_batch_device(gtd_handle h, const gtd_graph_desc* descs, int count,
+                                     const uint64_t* d_adj_pool, int64_t pool_len, int32_t* d_td,
+                                     int32_t* d_parent, const gtd_dp_batch_opts* opts) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  gtd_status s = check_descs(h, descs, count, pool_len);
+  if (s != GTD_OK)
+    return s;
+  if (!d_adj_pool || !d_td || !d_parent)
+    return fail(h, GTD_INVALID_ARG, "null pointer argument");
+  DeviceGuard g(h->device);
+  return batch_enqueue(h, descs, count, d_adj_pool, d_td, d_parent, opts);
+}
+
+gtd_status gtd_dp_batch_sync(gtd_handle h, gtd_dp_batch_stats* stats) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  DeviceGuard g(h->device);
+  return batch_finish(h, stats);
+}
+
+gtd_status gtd_dp_solve_batch(gtd_handle h, const gtd_graph_desc* descs, int count, const uint64_t* adj_pool,
+                              int64_t pool_len, int32_t* td_out, int32_t* parent_out,
+                              const gtd_dp_batch_opts* opts, gtd_dp_batch_stats* stats) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  gtd_status s = check_descs(h, descs, count, pool_len);
+  if (s != GTD_OK)
+    return s;
+  if (!adj_pool || !td_out || !parent_out)
+    return fail(h, GTD_INVALID_ARG, "null pointer argument");
+  for (int i = 0; i < count; ++i) {
+    s = check_adjacency(h, adj_pool + descs[i].offset, descs[i].n);
+    if (s != GTD_OK)
+      return fail(h, s, "graph " + std::to_string(i) + ": " + h->last_error);
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  DeviceGuard g(h->device);
+  const size_t adj_bytes = size_t(pool_len) * sizeof(uint64_t);
+  const size_t out_bytes = size_t(count) * sizeof(int32_t) + size_t(pool_len) * sizeof(int32_t);
+  s = grow_pinned(h, adj_bytes + out_bytes);
+  if (s != GTD_OK)
+    return s;
+  void* p = h->d_badj;
+  size_t cap = h->badj_cap * sizeof(uint64_t);
+  GTD_CUDA(h, ensure_device(&p, &cap, adj_bytes));
+  h->d_badj = static_cast<uint64_t*>(p);
+  h->badj_cap = cap / sizeof(uint64_t);
+  p = h->d_btd;
+  cap = h->btd_cap * sizeof(int32_t);
+  GTD_CUDA(h, ensure_device(&p, &cap, count * sizeof(int32_t)));
+  h->d_btd = static_cast<int32_t*>(p);
+  h->btd_cap = cap / sizeof(int32_t);
+  p = h->d_bparent;
+  cap = h->bparent_cap * sizeof(int32_t);
+  GTD_CUDA(h, ensure_device(&p, &cap, size_t(pool_len) * sizeof(int32_t)));
+  h->d_bparent = static_cast<int32_t*>(p);
+  h->bparent_cap = cap / sizeof(int32_t);
+
+  char* stage = static_cast<char*>(h->h_bstage);
+  std::memcpy(stage, adj_pool, adj_bytes);
+  GTD_CUDA(h, cudaMemcpyAsync(h->d_badj, stage, adj_bytes, cudaMemcpyHostToDevice, h->stream));
+  s = batch_enqueue(h, descs, count, h->d_badj, h->d_btd, h->d_bparent, opts);
+  if (s != GTD_OK)
+    return s;
+  int32_t* h_td = reinterpret_cast<int32_t*>(stage + adj_bytes);
+  int32_t* h_par = h_td + count;
+  GTD_CUDA(h, cudaMemcpyAsync(h_td, h->d_btd, count * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  GTD_CUDA(h, cudaMemcpyAsync(h_par, h->d_bparent, size_t(pool_len) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                              h->stream));
+  s = batch_finish(h, nullptr);
+  if (s != GTD_OK)
+    return s;
+  std::memcpy(td_out, h_td, count * sizeof(int32_t));
+  for (int i = 0; i < count; ++i)
+    std::memcpy(parent_out + descs[i].offset, h_par + descs[i].offset, descs[i].n * sizeof(int32_t));
+  h->bstats.total_ms =
+      std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats)
+    *stats = h->bstats;
+  return GTD_OK;
+}
+
+gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max, float* rates_out) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (n_min < 2 || n_max > 30 || n_min > n_max)
+    return fail(h, GTD_INVALID_ARG, "autotune range must lie in [2, 30]");
+  DeviceGuard g(h->device);
+  for (int n = n_min; n <= n_max; ++n) {
+    const int count = n >= 24 ? 1 : (1 << (24 - n));
+    std::vector<uint64_t> adj(size_t(count) * n);
+    std::vector<gtd_graph_desc> descs(count);
+    for (int i = 0; i < count; ++i) {
+      random_graph(n, uint64_t(n) * 1000003ull + i, adj.data() + size_t(i) * n);
+      descs[i].n = n;
+      descs[i].offset = i * n;
+    }
+    const int64_t pool = int64_t(count) * n;
+    std::vector<int32_t> td(count), par(pool);
+    for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb) {
+      gtd_dp_batch_opts o{lb, 0, 0, 1};
+      gtd_dp_batch_stats st{};
+      float best = 0;
+      for (int rep = 0; rep < 3; ++rep) {
+        gtd_status s = gtd_dp_solve_batch(h, descs.data(), count, adj.data(), pool, td.data(), par.data(), &o, &st);
+        if (s != GTD_OK)
+          return s;
+        if (rep > 0 && (best == 0 || st.dp_ms < best))
+          best = st.dp_ms;
+      }
+      const float rate = best > 0 ? float(double(st.subsets) / (best * 1000.0)) : 0.f;  // per microsecond
+      h->tune[n][lb] = rate;
+      if (rates_out)
+        rates_out[(n - n_min) * (kTuneLbMax - kTuneLbMin + 1) + (lb - kTuneLbMin)] = rate;
+    }
+  }
+  return GTD_OK;
+}
+
+}  // extern "C"

@@ -53,30 +53,13 @@ struct TileShape {
   static constexpr int kWords = kEntries / 4;   // 4 subsets per 32-bit word
   static constexpr int kWordBits = LB - 2;
   // dynamic shared memory: per warp T, MN, MX, CT (kWords words each), then
-  // the shared word order (kWords uint16) and the adjacency (kDpMaxN uint64).
+  // the shared word order (kWords uint16).
   static constexpr size_t kPerWarp = size_t(4) * kWords * 4;
   static constexpr size_t kOrderOff = size_t(kDpWarps) * kPerWarp;
-  static constexpr size_t kAdjOff = (kOrderOff + kWords * 2 + 15) & ~size_t(15);
-  static constexpr size_t kSmem = kAdjOff + kDpMaxN * 8;
+  static constexpr size_t kSmem = kOrderOff + kWords * 2;
 };
 
-// Checks the adjacency masks: no self loop, no bit >= n, symmetric.
-__device__ __forceinline__ bool adjacency_ok(const uint64_t* adj, int n) {
-  const uint64_t allowed = n >= 64 ? ~0ull : ((1ull << n) - 1);
-  for (int v = 0; v < n; ++v) {
-    uint64_t a = adj[v];
-    if ((a >> v) & 1ull)
-      return false;
-    if (a & ~allowed)
-      return false;
-    for (uint64_t s = a; s; s &= s - 1) {
-      int u = __ffsll(static_cast<long long>(s)) - 1;
-      if (!((adj[u] >> v) & 1ull))
-        return false;
-    }
-  }
-  return true;
-}
+using Binom = uint32_t[kDpMaxHigh + 1][kDpMaxHigh + 1];
 
 // Table bytes hold td << 1 | connected, so an unsigned min (max) over
 // children gives 2 * min td (2 * max td) plus a flag bit, without masking.
@@ -117,19 +100,11 @@ __device__ __forceinline__ void agg_add1(Agg& a, uint32_t x) {
 }
 
 // Scalar value of one subset from the min/max raw child bytes m, M, the
-// number c of connected children and k = |S|; s2 is S (used when k == 2).
-__device__ __forceinline__ uint32_t resolve(uint32_t m, uint32_t M, uint32_t c, int k, uint64_t s2,
-                                            const uint64_t* adj) {
+// number c of connected children and k = |S|; `adjacent` is used when k == 2.
+__device__ __forceinline__ uint32_t resolve(uint32_t m, uint32_t M, uint32_t c, int k, bool adjacent) {
   if (k <= 1)
     return k == 0 ? 0u : 3u;  // empty set: td 0; singleton: td 1, connected
-  bool conn;
-  if (k == 2) {
-    const int u = __ffsll(static_cast<long long>(s2)) - 1;
-    const int v = 63 - __clzll(static_cast<long long>(s2));
-    conn = (adj[u] >> v) & 1ull;
-  } else {
-    conn = c >= 2u;  // >= 2 non-cut vertices <=> connected (|S| >= 3)
-  }
+  const bool conn = k == 2 ? adjacent : c >= 2u;  // >= 2 non-cut vertices <=> connected
   return conn ? ((m & ~1u) + 3u) : (M & ~1u);
 }
 
@@ -141,9 +116,79 @@ __device__ __forceinline__ uint32_t resolve2(uint32_t mn, uint32_t mx, uint32_t 
   return (((mn & 0xFFFEFFFEu) + 0x00030003u) & m) | (mx & 0xFFFEFFFEu & ~m);
 }
 
+// Level j, high part H and level offsets of local tile t of a graph with nh
+// high vertices (level-major order, colex rank inside a level).
+__device__ __forceinline__ void decode_tile(const Binom& binom, int nh, uint32_t t, int& j, uint32_t& H,
+                                            uint32_t& off_prev) {
+  uint32_t off = 0, prev = 0;
+  j = 0;
+  while (off + binom[nh][j] <= t) {
+    prev = off;
+    off += binom[nh][j];
+    ++j;
+  }
+  off_prev = prev;
+  uint32_t r = t - off;
+  H = 0;
+  int k = j;
+  for (int a = nh - 1; k > 0; --a) {
+    const uint32_t c = binom[a][k];
+    if (r >= c) {
+      H |= 1u << a;
+      r -= c;
+      --k;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t rank_colex(const Binom& binom, uint32_t H) {
+  uint32_t r = 0;
+  int q = 0;
+  for (; H; H &= H - 1)
+    r += binom[__ffs(H) - 1][++q];
+  return r;
+}
+
+__device__ __forceinline__ bool adjacent_in(const uint64_t* adj, int n, uint64_t s2) {
+  const int u = __ffsll(static_cast<long long>(s2)) - 1;
+  const int v = 63 - __clzll(static_cast<long long>(s2));
+  return u < n && v < n && ((__ldg(adj + u) >> v) & 1ull);
+}
+
+// Checks one graph's adjacency masks: no self loop, no bit >= n, symmetric.
+__device__ bool adjacency_ok(const uint64_t* adj, int n) {
+  const uint64_t allowed = n >= 64 ? ~0ull : ((1ull << n) - 1);
+  for (int v = 0; v < n; ++v) {
+    const uint64_t a = adj[v];
+    if (((a >> v) & 1ull) || (a & ~allowed))
+      return false;
+    for (uint64_t s = a; s; s &= s - 1)
+      if (!((adj[__ffsll(static_cast<long long>(s)) - 1] >> v) & 1ull))
+        return false;
+  }
+  return true;
+}
+
+__global__ void dp_validate_kernel(const __grid_constant__ DpBatchParams p) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= p.num_graphs)
+    return;
+  const DpGraph G = p.graphs ? p.graphs[g] : p.single;
+  if (!adjacency_ok(p.adj + G.adj_off, G.n))
+    raise_error(p.error, kDevInvalidInput, g);
+}
+
+__global__ void dp_fill_tile_graph_kernel(const __grid_constant__ DpBatchParams p) {
+  for (int g = blockIdx.x; g < p.num_graphs; g += gridDim.x) {
+    const DpGraph G = p.graphs[g];
+    for (uint32_t t = threadIdx.x; t < G.ntiles; t += blockDim.x)
+      p.tile_graph[G.tile_base + t] = static_cast<uint32_t>(g);
+  }
+}
+
 template <int LB>
 __global__ void __launch_bounds__(32 * kDpWarps)
-    dp_tile_kernel(const DpKernelParams p) {
+    dp_tile_kernel(const __grid_constant__ DpBatchParams p) {
   using Shape = TileShape<LB>;
   constexpr int kWords = Shape::kWords;
   constexpr int kWordBits = Shape::kWordBits;
@@ -156,59 +201,39 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   uint32_t* MX = MN + kWords;
   uint32_t* CT = MX + kWords;
   uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + Shape::kOrderOff);
-  uint64_t* sAdj = reinterpret_cast<uint64_t*>(smem + Shape::kAdjOff);
-  __shared__ int sBadInput;
+  const Binom& binom = p.binom;
 
-  const DpLayout& lay = p.lay;
-  const int n = lay.n;
-  for (int v = threadIdx.x; v < n; v += blockDim.x)
-    sAdj[v] = p.adj[v];
   // Word indices ordered by popcount, colex rank inside each popcount class.
   for (int w = threadIdx.x; w < kWords; w += blockDim.x) {
     const int i = __popc(w);
     uint32_t pos = 0;
     for (int q = 0; q < i; ++q)
-      pos += lay.binom[kWordBits][q];
-    int m = 0;
-    for (uint32_t r = static_cast<uint32_t>(w); r; r &= r - 1)
-      pos += lay.binom[__ffs(r) - 1][++m];
+      pos += binom[kWordBits][q];
+    pos += rank_colex(binom, static_cast<uint32_t>(w));
     sOrder[pos] = static_cast<uint16_t>(w);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    sBadInput = adjacency_ok(sAdj, n) ? 0 : 1;
-    if (sBadInput)
-      raise_error(p.error, kDevInvalidInput, 0);
-  }
-  __syncthreads();
-  if (sBadInput)
-    return;
 
   for (;;) {
-    uint32_t t = 0;
-    if (lane == 0)
+    uint32_t t = 0, gi = 0;
+    if (lane == 0) {
       t = ld_relaxed_s32(p.error) != 0 ? 0xffffffffu : atomicAdd(p.ticket, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= lay.ntiles)
-      break;
-
-    // Level j and high part H of tile t (level-major, colex rank inside).
-    int j = 0;
-    while (lay.level_off[j + 1] <= t)
-      ++j;
-    uint32_t H = 0;
-    {
-      uint32_t r = t - lay.level_off[j];
-      int k = j;
-      for (int a = lay.nh - 1; k > 0; --a) {
-        const uint32_t c = lay.binom[a][k];
-        if (r >= c) {
-          H |= 1u << a;
-          r -= c;
-          --k;
-        }
-      }
+      if (t < p.total_tiles && p.graphs)
+        gi = __ldg(p.tile_graph + t);
     }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= p.total_tiles)
+      break;
+    gi = __shfl_sync(0xffffffffu, gi, 0);
+    const DpGraph G = p.graphs ? p.graphs[gi] : p.single;
+    const uint32_t tl = t - G.tile_base;
+    uint8_t* const table = p.table + G.table_off;
+    uint32_t* const flags = p.flags + G.tile_base;
+    const uint64_t* const adj = p.adj + G.adj_off;
+
+    int j;
+    uint32_t H, off_prev;
+    decode_tile(binom, G.nh, tl, j, H, off_prev);
 
     // Lane m < j owns child tile H - (m-th bit of H) and waits for it.
     uint32_t child = 0;
@@ -217,8 +242,8 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       uint32_t rest = H;
       for (int q = 0; q < lane; ++q)
         rest &= rest - 1;
-      child = lay.level_off[j - 1] + lay.rank_high(H & ~(rest & (0u - rest)));
-      ok = wait_flag(p.flags + child, p.epoch, p.timeout_ns, p.error);
+      child = off_prev + rank_colex(binom, H & ~(rest & (0u - rest)));
+      ok = wait_flag(flags + child, p.epoch, p.timeout_ns, p.error);
     }
     if (__any_sync(0xffffffffu, !ok))
       break;
@@ -236,8 +261,8 @@ __global__ void __launch_bounds__(32 * kDpWarps)
         for (; m + 2 <= j; m += 2) {
           const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
           const uint32_t c_b = __shfl_sync(0xffffffffu, child, m + 1);
-          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
-          const uint4 b = __ldcg(reinterpret_cast<const uint4*>(p.table + (size_t(c_b) << LB)) + (c0 >> 2) + lane);
+          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
+          const uint4 b = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_b) << LB)) + (c0 >> 2) + lane);
           agg_add2(g[0], a.x, b.x);
           agg_add2(g[1], a.y, b.y);
           agg_add2(g[2], a.z, b.z);
@@ -245,7 +270,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
         }
         if (m < j) {
           const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
-          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(p.table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
+          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
           agg_add1(g[0], a.x);
           agg_add1(g[1], a.y);
           agg_add1(g[2], a.z);
@@ -265,7 +290,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
         agg_init(g);
         for (int m = 0; m < j; ++m) {
           const uint32_t c_a = __shfl_sync(__activemask(), child, m);
-          agg_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(p.table + (size_t(c_a) << LB)) + w));
+          agg_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(table + (size_t(c_a) << LB)) + w));
         }
         MN[w] = pack16(g.mnl, g.mnh);
         MX[w] = pack16(g.mxl, g.mxh);
@@ -280,7 +305,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
     uint32_t start = 0;
 #pragma unroll 1
     for (int s = 0; s <= kWordBits; ++s) {
-      const uint32_t count = lay.binom[kWordBits][s];
+      const uint32_t count = binom[kWordBits][s];
       for (uint32_t e = lane; e < count; e += 32) {
         const uint32_t w = sOrder[start + e];
         const uint32_t mnp = MN[w], mxp = MX[w];
@@ -317,13 +342,17 @@ __global__ void __launch_bounds__(32 * kDpWarps)
           // small subsets (|S| <= 2 possible): one byte at a time
           const uint32_t mn = pack16(g.mnl, g.mnh), mx = pack16(g.mxl, g.mxh), ct = g.ct;
           const uint64_t S0 = Hfull | (uint64_t(w) << 2);
-          const uint32_t v0 = resolve(mn & 0xFFu, mx & 0xFFu, ct & 0xFFu, k, S0, sAdj);
+          const int n = G.n;
+          const uint32_t v0 = resolve(mn & 0xFFu, mx & 0xFFu, ct & 0xFFu, k, k == 2 && adjacent_in(adj, n, S0));
           const uint32_t v1 = resolve(min((mn >> 8) & 0xFFu, v0), max((mx >> 8) & 0xFFu, v0),
-                                      ((ct >> 8) & 0xFFu) + (v0 & 1u), k + 1, S0 | 1u, sAdj);
+                                      ((ct >> 8) & 0xFFu) + (v0 & 1u), k + 1,
+                                      k + 1 == 2 && adjacent_in(adj, n, S0 | 1u));
           const uint32_t v2 = resolve(min((mn >> 16) & 0xFFu, v0), max((mx >> 16) & 0xFFu, v0),
-                                      ((ct >> 16) & 0xFFu) + (v0 & 1u), k + 1, S0 | 2u, sAdj);
+                                      ((ct >> 16) & 0xFFu) + (v0 & 1u), k + 1,
+                                      k + 1 == 2 && adjacent_in(adj, n, S0 | 2u));
           const uint32_t v3 = resolve(min(min(mn >> 24, v1), v2), max(max(mx >> 24, v1), v2),
-                                      (ct >> 24) + (v1 & 1u) + (v2 & 1u), k + 2, S0 | 3u, sAdj);
+                                      (ct >> 24) + (v1 & 1u) + (v2 & 1u), k + 2,
+                                      k + 2 == 2 && adjacent_in(adj, n, S0 | 3u));
           T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
         }
       }
@@ -332,7 +361,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
     }
 
     // Store the tile, then publish it.
-    uint32_t* dst = reinterpret_cast<uint32_t*>(p.table + (size_t(t) << LB));
+    uint32_t* dst = reinterpret_cast<uint32_t*>(table + (size_t(tl) << LB));
     if constexpr (kWords >= 128) {
       for (int w4 = lane; w4 < kWords / 4; w4 += 32)
         reinterpret_cast<uint4*>(dst)[w4] = reinterpret_cast<const uint4*>(T)[w4];
@@ -348,8 +377,10 @@ __global__ void __launch_bounds__(32 * kDpWarps)
 }
 
 // ---------------------------------------------------------------------------
-// Reconstruction: one warp; lanes cover vertices lane and lane + 32.
+// Reconstruction: one warp per graph; lanes cover vertices lane, lane + 32.
 // ---------------------------------------------------------------------------
+
+constexpr int kTreeWarps = 4;
 
 __device__ __forceinline__ uint64_t ballot64(bool lo, bool hi) {
   const uint32_t a = __ballot_sync(0xffffffffu, lo);
@@ -378,116 +409,140 @@ __device__ uint64_t warp_component(uint64_t S, int v, const uint64_t* adj, int n
   return reach;
 }
 
-__device__ __forceinline__ uint32_t td_of(const DpKernelParams& p, uint64_t S) {
-  return p.table[p.lay.index(S)] >> 1;
-}
+struct TreeCtx {
+  const Binom& binom;
+  const uint8_t* table;
+  int lb, nh, n;
+  __device__ uint32_t td_of(uint64_t S) const {
+    const uint32_t H = static_cast<uint32_t>(S >> lb);
+    const int j = __popc(H);
+    uint32_t off = 0;
+    for (int i = 0; i < j; ++i)
+      off += binom[nh][i];
+    const uint64_t tile = off + rank_colex(binom, H);
+    return table[(tile << lb) | (S & ((1ull << lb) - 1))] >> 1;
+  }
+  // First vertex v of the connected set C with td(C - v) = td(C) - 1.
+  __device__ int root(uint64_t C) const {
+    if (__popcll(C) == 1)
+      return __ffsll(static_cast<long long>(C)) - 1;
+    const int lane = threadIdx.x & 31;
+    const uint32_t want = td_of(C) - 1u;
+    bool hit_lo = false, hit_hi = false;
+    if ((C >> lane) & 1ull)
+      hit_lo = td_of(C & ~(1ull << lane)) == want;
+    if (lane + 32 < n && ((C >> (lane + 32)) & 1ull))
+      hit_hi = td_of(C & ~(1ull << (lane + 32))) == want;
+    const uint64_t hits = ballot64(hit_lo, hit_hi);
+    return hits ? __ffsll(static_cast<long long>(hits)) - 1 : -1;
+  }
+};
 
-// First vertex v of the connected set C with td(C - v) = td(C) - 1.
-__device__ int warp_root(const DpKernelParams& p, uint64_t C) {
-  if (__popcll(C) == 1)
-    return __ffsll(static_cast<long long>(C)) - 1;
-  const int lane = threadIdx.x & 31;
-  const uint32_t want = td_of(p, C) - 1u;
-  bool hit_lo = false, hit_hi = false;
-  if ((C >> lane) & 1ull)
-    hit_lo = td_of(p, C & ~(1ull << lane)) == want;
-  if (lane + 32 < p.lay.n && ((C >> (lane + 32)) & 1ull))
-    hit_hi = td_of(p, C & ~(1ull << (lane + 32))) == want;
-  const uint64_t hits = ballot64(hit_lo, hit_hi);
-  return hits ? __ffsll(static_cast<long long>(hits)) - 1 : -1;
-}
-
-__global__ void __launch_bounds__(32)
-    dp_tree_kernel(const DpKernelParams p, uint64_t query, int32_t* td_out,
-                   int32_t* parent_out, int32_t* order_out) {
-  __shared__ uint64_t sAdj[kDpMaxN];
-  __shared__ uint64_t stMask[kDpMaxN];
-  __shared__ int32_t stOwner[kDpMaxN];
-  __shared__ int32_t stDepth[kDpMaxN];
-  const int lane = threadIdx.x;
-  const int n = p.lay.n;
-  for (int v = lane; v < n; v += 32)
-    sAdj[v] = p.adj[v];
-  __syncwarp();
+__global__ void __launch_bounds__(32 * kTreeWarps)
+    dp_tree_kernel(const __grid_constant__ DpBatchParams p) {
+  __shared__ uint64_t sAdjAll[kTreeWarps][kDpMaxN];
+  __shared__ uint64_t stMaskAll[kTreeWarps][kDpMaxN];
+  __shared__ int32_t stOwnerAll[kTreeWarps][kDpMaxN];
+  __shared__ int32_t stDepthAll[kTreeWarps][kDpMaxN];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t* sAdj = sAdjAll[warp];
+  uint64_t* stMask = stMaskAll[warp];
+  int32_t* stOwner = stOwnerAll[warp];
+  int32_t* stDepth = stDepthAll[warp];
   if (ld_relaxed_s32(p.error) != 0)
     return;
 
-  const uint32_t td = query ? td_of(p, query) : 0u;
-  if (lane == 0 && td_out)
-    *td_out = static_cast<int32_t>(td);
-
-  if (parent_out) {
-    // Canonical tree: every component is rooted at warp_root and its
-    // sub-components hang below that root (dynamic_cpu.hpp:59-81).
-    int top = 0, height = 0;
-    for (uint64_t rest = query; rest;) {
-      const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
-      rest &= ~c;
-      if (lane == 0) {
-        stMask[top] = c;
-        stOwner[top] = -1;
-        stDepth[top] = 1;
-      }
-      ++top;
-    }
+  for (int g = blockIdx.x * kTreeWarps + warp; g < p.num_graphs; g += gridDim.x * kTreeWarps) {
+    const DpGraph G = p.graphs ? p.graphs[g] : p.single;
+    const int n = G.n;
+    for (int v = lane; v < n; v += 32)
+      sAdj[v] = p.adj[G.adj_off + v];
     __syncwarp();
-    while (top > 0) {
-      --top;
-      const uint64_t C = stMask[top];
-      const int owner = stOwner[top], depth = stDepth[top];
-      __syncwarp();
-      const int r = warp_root(p, C);
-      if (r < 0) {
-        if (lane == 0)
-          raise_error(p.error, kDevNoRoot, static_cast<int32_t>(__popcll(C)));
-        return;
-      }
-      if (lane == 0)
-        parent_out[r] = owner;
-      height = max(height, depth);
-      for (uint64_t rest = C & ~(1ull << r); rest;) {
+    const TreeCtx ctx{p.binom, p.table + G.table_off, p.lb, G.nh, n};
+    const uint64_t query = p.query ? p.query : (n == 64 ? ~0ull : ((1ull << n) - 1));
+    const uint32_t td = query ? ctx.td_of(query) : 0u;
+    if (lane == 0 && p.td_out)
+      p.td_out[G.out_idx] = static_cast<int32_t>(td);
+
+    if (p.parent_out) {
+      // Canonical tree: every component is rooted at ctx.root and its
+      // sub-components hang below that root (dynamic_cpu.hpp:59-81).
+      int32_t* parent = p.parent_out + G.adj_off;
+      int top = 0, height = 0;
+      for (uint64_t rest = query; rest;) {
         const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
         rest &= ~c;
         if (lane == 0) {
           stMask[top] = c;
-          stOwner[top] = r;
-          stDepth[top] = depth + 1;
+          stOwner[top] = -1;
+          stDepth[top] = 1;
         }
         ++top;
       }
       __syncwarp();
-    }
-    if (static_cast<uint32_t>(height) != td && lane == 0)
-      raise_error(p.error, kDevNoRoot, -1);
-  }
-
-  if (order_out) {
-    // GetElimination (dynamic_gpu.hpp:58-63): repeatedly remove the stored
-    // root of the remaining set; for a disconnected set that is the root of
-    // its first deepest component (dynamic_gpu.cu:92-103).
-    uint64_t R = query;
-    for (int step = 0; R; ++step) {
-      uint64_t best = 0;
-      uint32_t best_td = 0;
-      for (uint64_t rest = R; rest;) {
-        const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
-        rest &= ~c;
-        const uint32_t t = td_of(p, c);
-        if (best == 0 || t > best_td) {
-          best = c;
-          best_td = t;
+      while (top > 0) {
+        --top;
+        const uint64_t C = stMask[top];
+        const int owner = stOwner[top], depth = stDepth[top];
+        __syncwarp();
+        const int r = ctx.root(C);
+        if (r < 0) {
+          if (lane == 0)
+            raise_error(p.error, kDevNoRoot, g);
+          return;
         }
-      }
-      const int r = warp_root(p, best);
-      if (r < 0) {
         if (lane == 0)
-          raise_error(p.error, kDevNoRoot, -2);
+          parent[r] = owner;
+        height = max(height, depth);
+        for (uint64_t rest = C & ~(1ull << r); rest;) {
+          const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
+          rest &= ~c;
+          if (lane == 0) {
+            stMask[top] = c;
+            stOwner[top] = r;
+            stDepth[top] = depth + 1;
+          }
+          ++top;
+        }
+        __syncwarp();
+      }
+      if (static_cast<uint32_t>(height) != td) {
+        if (lane == 0)
+          raise_error(p.error, kDevNoRoot, g);
         return;
       }
-      if (lane == 0)
-        order_out[step] = r;
-      R &= ~(1ull << r);
     }
+
+    if (p.order_out) {
+      // GetElimination (dynamic_gpu.hpp:58-63): repeatedly remove the stored
+      // root of the remaining set; for a disconnected set that is the root of
+      // its first deepest component (dynamic_gpu.cu:92-103).
+      int32_t* order = p.order_out + G.adj_off;
+      uint64_t R = query;
+      for (int step = 0; R; ++step) {
+        uint64_t best = 0;
+        uint32_t best_td = 0;
+        for (uint64_t rest = R; rest;) {
+          const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
+          rest &= ~c;
+          const uint32_t t = ctx.td_of(c);
+          if (best == 0 || t > best_td) {
+            best = c;
+            best_td = t;
+          }
+        }
+        const int r = ctx.root(best);
+        if (r < 0) {
+          if (lane == 0)
+            raise_error(p.error, kDevNoRoot, g);
+          return;
+        }
+        if (lane == 0)
+          order[step] = r;
+        R &= ~(1ull << r);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -495,8 +550,18 @@ __global__ void __launch_bounds__(32)
 // Host-side launch helpers.
 // ---------------------------------------------------------------------------
 
+void dp_fill_binom(DpBatchParams& p) {
+  for (int a = 0; a <= kDpMaxHigh; ++a) {
+    for (int b = 0; b <= kDpMaxHigh; ++b)
+      p.binom[a][b] = 0;
+    p.binom[a][0] = 1;
+    for (int b = 1; b <= a; ++b)
+      p.binom[a][b] = p.binom[a - 1][b - 1] + (b <= a - 1 ? p.binom[a - 1][b] : 0u);
+  }
+}
+
 template <int LB>
-static cudaError_t launch_tiles(const DpKernelParams& p, int ctas, cudaStream_t s) {
+static cudaError_t launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s) {
   dp_tile_kernel<LB><<<ctas, 32 * kDpWarps, TileShape<LB>::kSmem, s>>>(p);
   return cudaGetLastError();
 }
@@ -512,11 +577,6 @@ static int occupancy_tiles() {
   return blocks;
 }
 
-int dp_tile_threads(int lb) {
-  (void)lb;
-  return 32 * kDpWarps;
-}
-
 int dp_tile_occupancy(int lb) {
   switch (lb) {
 #define GTD_CASE(X) \
@@ -530,8 +590,19 @@ int dp_tile_occupancy(int lb) {
   }
 }
 
-cudaError_t dp_launch_tiles(const DpKernelParams& p, int ctas, cudaStream_t s) {
-  switch (p.lay.lb) {
+cudaError_t dp_launch_validate(const DpBatchParams& p, cudaStream_t s) {
+  dp_validate_kernel<<<(p.num_graphs + 127) / 128, 128, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t dp_launch_fill_tile_graph(const DpBatchParams& p, cudaStream_t s) {
+  const int blocks = p.num_graphs < 4096 ? p.num_graphs : 4096;
+  dp_fill_tile_graph_kernel<<<blocks, 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t dp_launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s) {
+  switch (p.lb) {
 #define GTD_CASE(X) \
   case X:           \
     return launch_tiles<X>(p, ctas, s);
@@ -543,9 +614,11 @@ cudaError_t dp_launch_tiles(const DpKernelParams& p, int ctas, cudaStream_t s) {
   }
 }
 
-cudaError_t dp_launch_tree(const DpKernelParams& p, uint64_t query, int32_t* td,
-                           int32_t* parent, int32_t* order, cudaStream_t s) {
-  dp_tree_kernel<<<1, 32, 0, s>>>(p, query, td, parent, order);
+cudaError_t dp_launch_tree(const DpBatchParams& p, cudaStream_t s) {
+  int blocks = (p.num_graphs + kTreeWarps - 1) / kTreeWarps;
+  if (blocks > 4096)
+    blocks = 4096;
+  dp_tree_kernel<<<blocks, 32 * kTreeWarps, 0, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -9,23 +9,49 @@
 
 namespace gtd {
 
-// Passed by value (it lives in the kernel parameter bank, so the binomial
-// table and level offsets are read through the constant cache).
-struct DpKernelParams {
-  DpLayout lay;
-  uint8_t* table = nullptr;        // 2^n bytes
-  uint32_t* flags = nullptr;       // one ready stamp per tile
-  uint32_t* ticket = nullptr;      // work counter, zeroed before each launch
-  int32_t* error = nullptr;        // [0] code, [1] info
-  const uint64_t* adj = nullptr;   // n masks, device memory
-  uint32_t epoch = 0;              // flags equal to epoch are ready
-  uint64_t timeout_ns = 0;         // bound of every dependency wait
+// One graph of a DP launch (32 bytes). A graph with n < lb is padded with
+// isolated vertices up to lb (one tile); padding changes no treedepth of a
+// real subset and the reconstruction never touches padded vertices.
+struct DpGraph {
+  uint64_t table_off = 0;  // byte offset of the graph's table in the table pool
+  uint32_t tile_base = 0;  // first global tile (ticket) of the graph
+  uint32_t ntiles = 0;     // 2^nh
+  uint32_t adj_off = 0;    // first adjacency mask; also the first output slot
+  int32_t n = 0;           // real vertices
+  int32_t nh = 0;          // high vertices (max(n - lb, 0))
+  int32_t out_idx = 0;     // position of the graph in the caller's arrays (td_out)
 };
 
-int dp_tile_threads(int lb);
+// Passed by value as a __grid_constant__ kernel parameter: the binomial
+// table is read through the constant cache.
+struct DpBatchParams {
+  uint32_t binom[kDpMaxHigh + 1][kDpMaxHigh + 1] = {};  // C(a, b)
+  const DpGraph* graphs = nullptr;  // device descriptors; nullptr: only `single`
+  DpGraph single;
+  uint32_t* tile_graph = nullptr;   // graph index of every global tile (batches)
+  int num_graphs = 1;
+  int lb = 0;                       // tile bits of this launch
+  uint32_t total_tiles = 0;
+  uint8_t* table = nullptr;         // table pool
+  uint32_t* flags = nullptr;        // one ready stamp per global tile
+  uint32_t* ticket = nullptr;       // work counter, zeroed before each launch
+  int32_t* error = nullptr;         // [0] code, [1] info
+  const uint64_t* adj = nullptr;    // adjacency pool (device)
+  uint32_t epoch = 0;               // flags equal to epoch are ready
+  uint64_t timeout_ns = 0;          // bound of every dependency wait
+  // reconstruction outputs (device): td_out[g], parent_out[adj_off + v],
+  // order_out[adj_off + step]; query != 0 restricts a single graph to a subset
+  uint64_t query = 0;
+  int32_t* td_out = nullptr;
+  int32_t* parent_out = nullptr;
+  int32_t* order_out = nullptr;
+};
+
+void dp_fill_binom(DpBatchParams& p);
 int dp_tile_occupancy(int lb);
-cudaError_t dp_launch_tiles(const DpKernelParams& p, int ctas, cudaStream_t s);
-cudaError_t dp_launch_tree(const DpKernelParams& p, uint64_t query, int32_t* td,
-                           int32_t* parent, int32_t* order, cudaStream_t s);
+cudaError_t dp_launch_validate(const DpBatchParams& p, cudaStream_t s);
+cudaError_t dp_launch_fill_tile_graph(const DpBatchParams& p, cudaStream_t s);
+cudaError_t dp_launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s);
+cudaError_t dp_launch_tree(const DpBatchParams& p, cudaStream_t s);
 
 }  // namespace gtd

@@ -1,4 +1,4 @@
-// Handle state shared by the C-ABI translation units (host only).
+// Handle state and helpers shared by the C-ABI translation units (host only).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -7,6 +7,7 @@
 #include <string>
 
 #include "../../include/gtd.h"
+#include "gtd_device.cuh"
 #include "gtd_dp_kernels.h"
 
 namespace gtd {
@@ -21,6 +22,12 @@ constexpr int kIoParent = 8;
 constexpr int kIoOrder = 72;
 constexpr int kIoWords = 256;
 
+// Flag stamp reserved for CUDA-graph replays (the graph zeroes the flags
+// first); direct launches cycle their epochs through [1, kGraphEpoch).
+constexpr uint32_t kGraphEpoch = 0xFFFFFFFEu;
+constexpr int kTuneLbMin = 8;
+constexpr int kTuneLbMax = 12;
+
 }  // namespace gtd
 
 struct gtd_handle_s {
@@ -30,7 +37,7 @@ struct gtd_handle_s {
   bool own_stream = false;
   std::string last_error;
 
-  // Subset DP buffers.
+  // Subset DP buffers (shared by single and batched solves).
   uint8_t* d_table = nullptr;
   size_t table_cap = 0;
   uint32_t* d_flags = nullptr;
@@ -41,14 +48,69 @@ struct gtd_handle_s {
   void* h_pinned = nullptr;  // staging for adj (in) and the IO block (out)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
+  // Batched DP buffers.
+  gtd::DpGraph* d_bgraphs = nullptr;
+  size_t bgraphs_cap = 0;
+  uint32_t* d_tile_graph = nullptr;
+  size_t tile_graph_cap = 0;
+  uint64_t* d_badj = nullptr;
+  size_t badj_cap = 0;
+  int32_t* d_btd = nullptr;
+  size_t btd_cap = 0;
+  int32_t* d_bparent = nullptr;
+  size_t bparent_cap = 0;
+  void* h_bstage = nullptr;  // pinned: adjacency pool in, td + parent out
+  size_t bstage_cap = 0;
+  cudaGraphExec_t bgraph = nullptr;
+  uint64_t bgraph_key = 0;
+  bool bgraph_valid = false;
+  gtd::DpBatchParams bparams;
+  gtd_dp_batch_stats bstats = {};
+  // Autotuner: subsets per millisecond by n and tile bits (0 = unmeasured).
+  float tune[GTD_DP_MAX_N + 1][gtd::kTuneLbMax + 1] = {};
+
   // Last DP solve (for gtd_dp_query / gtd_sync).
   bool have_table = false;
   bool pending_stats = false;
-  gtd::DpKernelParams last_params;
+  gtd::DpBatchParams last_params;
   gtd_dp_stats last_stats = {};
 };
 
 namespace gtd {
+
 gtd_status fail(gtd_handle h, gtd_status s, const std::string& msg);
 gtd_status cuda_fail(gtd_handle h, cudaError_t e, const char* what);
+gtd_status check_adjacency(gtd_handle h, const uint64_t* adj, int n);
+gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info);
+// Grows a device buffer to at least `bytes` (contents not kept).
+cudaError_t ensure_device(void** ptr, size_t* cap, size_t bytes);
+// Grows the flag array; fresh flags are zeroed and the epoch restarts.
+gtd_status ensure_flags(gtd_handle h, size_t tiles);
+// Next epoch for a direct (non-graph) launch.
+gtd_status next_epoch(gtd_handle h, uint32_t* epoch);
+
+// Makes the handle's device current for the duration of a call and restores
+// the caller's device afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess)
+      prev = -1;
+    if (prev != dev)
+      cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+      cudaSetDevice(prev);
+  }
+};
+
 }  // namespace gtd
+
+#define GTD_CUDA(h, call)                      \
+  do {                                         \
+    cudaError_t e_ = (call);                   \
+    if (e_ != cudaSuccess)                     \
+      return ::gtd::cuda_fail((h), e_, #call); \
+  } while (0)

@@ -107,10 +107,17 @@ extern "C" gtd_status gtd_dp_solve_noalloc(const uint64_t* d_adj, int n, int32_t
     return GTD_CUDA_ERROR;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
-  DpKernelParams p;
-  p.lay = make_dp_layout(n, kNoallocTileBits);
-  if (p.lay.ntiles > kNoallocMaxTiles)
+  const DpLayout L = make_dp_layout(n, kNoallocTileBits);
+  if (L.ntiles > kNoallocMaxTiles)
     return GTD_INVALID_ARG;
+  DpBatchParams p;
+  dp_fill_binom(p);
+  p.single.ntiles = L.ntiles;
+  p.single.n = n;
+  p.single.nh = L.nh;
+  p.num_graphs = 1;
+  p.lb = L.lb;
+  p.total_tiles = L.ntiles;
   p.table = base;
   p.flags = reinterpret_cast<uint32_t*>(base + kNoallocFlagsOffset);
   int32_t* ctrl = reinterpret_cast<int32_t*>(base + kNoallocCtrlOffset);
@@ -118,6 +125,9 @@ extern "C" gtd_status gtd_dp_solve_noalloc(const uint64_t* d_adj, int n, int32_t
   p.error = ctrl + 1;
   p.adj = d_adj;
   p.timeout_ns = 10ull * 1000 * 1000 * 1000;
+  p.td_out = d_td;
+  p.parent_out = d_parent;
+  p.order_out = d_order;
   uint32_t epoch = g_epoch[dev].fetch_add(1) + 1;
   if (epoch == 0 || epoch == 0xffffffffu) {
     // wrapped: clear every flag so that no stale stamp matches
@@ -128,18 +138,19 @@ extern "C" gtd_status gtd_dp_solve_noalloc(const uint64_t* d_adj, int n, int32_t
   }
   p.epoch = epoch;
 
-  int occ = dp_tile_occupancy(p.lay.lb);
+  int occ = dp_tile_occupancy(p.lb);
   if (occ < 1)
     occ = 1;
   long long ctas = static_cast<long long>(g_num_sms[dev]) * occ;
-  if (ctas > p.lay.ntiles)
-    ctas = p.lay.ntiles;
+  if (ctas > p.total_tiles)
+    ctas = p.total_tiles;
   if (cudaMemsetAsync(ctrl, 0, 4 * sizeof(int32_t), s) != cudaSuccess)
+    return GTD_CUDA_ERROR;
+  if (dp_launch_validate(p, s) != cudaSuccess)
     return GTD_CUDA_ERROR;
   if (dp_launch_tiles(p, static_cast<int>(ctas), s) != cudaSuccess)
     return GTD_CUDA_ERROR;
-  const uint64_t full = (1ull << n) - 1;
-  if (dp_launch_tree(p, full, d_td, d_parent, d_order, s) != cudaSuccess)
+  if (dp_launch_tree(p, s) != cudaSuccess)
     return GTD_CUDA_ERROR;
   int32_t code = 0;
   if (cudaMemcpyAsync(&code, p.error, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess)

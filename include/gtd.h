@@ -110,6 +110,68 @@ uint64_t gtd_dp_table_index(int n, int tile_bits, uint64_t subset_mask);
  * memory `out` of `bytes` bytes. */
 gtd_status gtd_dp_read_table(gtd_handle h, uint8_t* out, uint64_t bytes);
 
+/* ---- Batched subset DP ------------------------------------------------ */
+
+/* One graph of a batch: n vertices; its adjacency masks are
+ * adj_pool[offset .. offset + n) and its parent array is written to
+ * parent_out[offset .. offset + n). */
+typedef struct {
+  int32_t n;
+  int32_t offset;
+} gtd_graph_desc;
+
+typedef struct {
+  int tile_bits;        /* 8..12; 0 = from gtd_dp_autotune, else 10 */
+  int ctas_per_sm;      /* 0 = occupancy limit */
+  uint64_t timeout_ns;  /* bound on every in-kernel wait (0 = 10 s) */
+  int use_cuda_graph;   /* capture the launch once, replay while the batch
+                           (sizes, offsets, buffers) stays the same */
+} gtd_dp_batch_opts;
+
+typedef struct {
+  float dp_ms;          /* device time of validate + DP + tree, CUDA events */
+  float total_ms;       /* whole call including copies */
+  uint64_t subsets;     /* sum of 2^n over the batch */
+  uint64_t alg_bytes;   /* sum of 2^n + n 2^(n-1) */
+  uint64_t table_bytes; /* table pool (graphs with n < tile bits padded) */
+  int tile_bits;
+  int tiles;
+  int ctas;
+  int graph_replayed;   /* 1 if an existing CUDA graph was replayed */
+} gtd_dp_batch_stats;
+
+/* DynamicGPU over many graphs of uneven size in ONE persistent launch
+ * (every graph's tiles in one ticket order, largest graphs first), the
+ * launch sequence optionally captured in a CUDA graph. Results are those of
+ * gtd_dp_solve for every graph: td_out[i], and the tree of graph i in
+ * parent_out[descs[i].offset ...]. Host pointers; adj_pool and parent_out
+ * hold pool_len entries. 1 <= n <= GTD_DP_MAX_N per graph. */
+gtd_status gtd_dp_solve_batch(gtd_handle h, const gtd_graph_desc* descs,
+                              int count, const uint64_t* adj_pool,
+                              int64_t pool_len, int32_t* td_out,
+                              int32_t* parent_out,
+                              const gtd_dp_batch_opts* opts,
+                              gtd_dp_batch_stats* stats);
+
+/* The same with adjacency pool and outputs in DEVICE memory (descs stay on
+ * the host); enqueued on the handle's stream; gtd_dp_batch_sync waits,
+ * reports in-kernel errors and fills the stats. */
+gtd_status gtd_dp_solve_batch_device(gtd_handle h, const gtd_graph_desc* descs,
+                                     int count, const uint64_t* d_adj_pool,
+                                     int64_t pool_len, int32_t* d_td,
+                                     int32_t* d_parent,
+                                     const gtd_dp_batch_opts* opts);
+gtd_status gtd_dp_batch_sync(gtd_handle h, gtd_dp_batch_stats* stats);
+
+/* The autotuner: times the batched DP kernel for every n in [n_min, n_max]
+ * and tile bits 8..12 on seeded random graphs (about 2^24 subsets per
+ * measurement) and keeps the rates in the handle; batches solved with
+ * tile_bits = 0 then use the tile size with the least predicted time.
+ * rates_out (may be NULL) receives (n_max - n_min + 1) x 5 rates in subsets
+ * per microsecond, row n, column tile bits - 8. */
+gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max,
+                           float* rates_out);
+
 /* Largest n gtd_dp_solve_noalloc accepts (its fixed scratch holds a 2^n-byte
  * table: 16 MiB at n = 24). */
 #define GTD_DP_NOALLOC_MAX_N 24
