@@ -267,7 +267,8 @@ gtd_status gtd_destroy(gtd_handle h) {
     cudaFree(h->d_io);
     cudaFree(h->d_adj);
     cudaFree(h->d_bgraphs);
-    cudaFree(h->d_tile_graph);
+    cudaFree(h->d_tile_map);
+    cudaFree(h->d_level_base);
     cudaFree(h->d_badj);
     cudaFree(h->d_btd);
     cudaFree(h->d_bparent);

@@ -1,9 +1,10 @@
 // Batched subset DP: many graphs of uneven size in one persistent launch.
 //
-// Planning (host): graphs are put in descending n (largest first, so the
-// tail of the launch is made of small graphs), each gets a table region, a
-// tile range in the global ticket order and a descriptor; the tile->graph
-// lookup is filled on the device. The launch sequence (zero the flags and
+// Planning (host): graphs are put in descending n, each gets a table region,
+// a flag range and a descriptor. Tickets run level-major across graphs
+// (level 0 of every graph, then level 1, ...), so the children a tile waits
+// for were issued long before it; the ticket -> (graph, tile) map is filled
+// on the device. The launch sequence (zero the flags and
 // control words, validate, DP, tree) is captured once in a CUDA graph and
 // replayed while the batch keeps its shape and buffers.
 //
@@ -31,7 +32,10 @@ struct Plan {
   uint32_t total_tiles = 0;
   uint64_t subsets = 0;
   uint64_t alg_bytes = 0;
+  std::vector<uint32_t> level_base;  // [graph][level]: first ticket of that level
 };
+
+constexpr int kLevelSlots = kDpMaxHigh + 2;
 
 int pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const gtd_dp_batch_opts* opts) {
   if (opts && opts->tile_bits > 0)
@@ -83,6 +87,23 @@ Plan make_plan(int lb, const gtd_graph_desc* descs, int count) {
   }
   P.table_bytes = off;
   P.total_tiles = tile;
+  // Tickets level-major across graphs: level 0 of every graph, then level 1...
+  P.level_base.assign(size_t(count) * kLevelSlots, 0);
+  uint32_t binom[kDpMaxHigh + 1][kDpMaxHigh + 1] = {};
+  for (int a = 0; a <= kDpMaxHigh; ++a) {
+    binom[a][0] = 1;
+    for (int b = 1; b <= a; ++b)
+      binom[a][b] = binom[a - 1][b - 1] + (b <= a - 1 ? binom[a - 1][b] : 0u);
+  }
+  uint32_t ticket = 0;
+  for (int j = 0; j <= kDpMaxHigh; ++j)
+    for (int k = 0; k < count; ++k) {
+      const DpGraph& G = P.graphs[k];
+      if (j <= G.nh) {
+        P.level_base[size_t(k) * kLevelSlots + j] = ticket;
+        ticket += binom[G.nh][j];
+      }
+    }
   return P;
 }
 
@@ -165,22 +186,32 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   gtd_status s = ensure_flags(h, P.total_tiles);
   if (s != GTD_OK)
     return s;
-  p = h->d_tile_graph;
-  size_t cap = h->tile_graph_cap * sizeof(uint32_t);
-  GTD_CUDA(h, ensure_device(&p, &cap, P.total_tiles * sizeof(uint32_t)));
-  h->d_tile_graph = static_cast<uint32_t*>(p);
-  h->tile_graph_cap = cap / sizeof(uint32_t);
+  p = h->d_tile_map;
+  size_t cap = h->tile_map_cap * sizeof(uint2);
+  GTD_CUDA(h, ensure_device(&p, &cap, P.total_tiles * sizeof(uint2)));
+  h->d_tile_map = static_cast<uint2*>(p);
+  h->tile_map_cap = cap / sizeof(uint2);
+  p = h->d_level_base;
+  cap = h->level_base_cap * sizeof(uint32_t);
+  GTD_CUDA(h, ensure_device(&p, &cap, P.level_base.size() * sizeof(uint32_t)));
+  h->d_level_base = static_cast<uint32_t*>(p);
+  h->level_base_cap = cap / sizeof(uint32_t);
   p = h->d_bgraphs;
   cap = h->bgraphs_cap * sizeof(DpGraph);
   GTD_CUDA(h, ensure_device(&p, &cap, count * sizeof(DpGraph)));
   h->d_bgraphs = static_cast<DpGraph*>(p);
   h->bgraphs_cap = cap / sizeof(DpGraph);
-  // Descriptors go up through pinned staging (synchronised below, so the
-  // staging can be reused right after).
+  // Descriptors and level bases go up through pinned staging (synchronised
+  // below, so the staging is released right after).
+  const size_t gbytes = count * sizeof(DpGraph), lbytes = P.level_base.size() * sizeof(uint32_t);
   void* stage = nullptr;
-  GTD_CUDA(h, cudaMallocHost(&stage, count * sizeof(DpGraph)));
-  std::memcpy(stage, P.graphs.data(), count * sizeof(DpGraph));
-  cudaError_t e = cudaMemcpyAsync(h->d_bgraphs, stage, count * sizeof(DpGraph), cudaMemcpyHostToDevice, h->stream);
+  GTD_CUDA(h, cudaMallocHost(&stage, gbytes + lbytes));
+  std::memcpy(stage, P.graphs.data(), gbytes);
+  std::memcpy(static_cast<char*>(stage) + gbytes, P.level_base.data(), lbytes);
+  cudaError_t e = cudaMemcpyAsync(h->d_bgraphs, stage, gbytes, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_level_base, static_cast<char*>(stage) + gbytes, lbytes, cudaMemcpyHostToDevice,
+                        h->stream);
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(h->stream);
   cudaFreeHost(stage);
@@ -190,7 +221,8 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   bp = DpBatchParams{};
   dp_fill_binom(bp);
   bp.graphs = h->d_bgraphs;
-  bp.tile_graph = h->d_tile_graph;
+  bp.tile_map = h->d_tile_map;
+  bp.level_base = h->d_level_base;
   bp.num_graphs = count;
   bp.lb = lb;
   bp.total_tiles = P.total_tiles;
@@ -202,7 +234,7 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   bp.timeout_ns = timeout;
   bp.td_out = d_td;
   bp.parent_out = d_parent;
-  GTD_CUDA(h, dp_launch_fill_tile_graph(bp, h->stream));
+  GTD_CUDA(h, dp_launch_fill_tile_map(bp, h->stream));
 
   if (use_graph) {
     if (h->bgraph) {
@@ -388,7 +420,7 @@ gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max, float* rates_out)
     return fail(h, GTD_INVALID_ARG, "autotune range must lie in [2, 30]");
   DeviceGuard g(h->device);
   for (int n = n_min; n <= n_max; ++n) {
-    const int count = n >= 24 ? 1 : (1 << (24 - n));
+    const int count = n >= 20 ? 64 : (1 << (26 - n));
     std::vector<uint64_t> adj(size_t(count) * n);
     std::vector<gtd_graph_desc> descs(count);
     for (int i = 0; i < count; ++i) {

@@ -178,11 +178,20 @@ __global__ void dp_validate_kernel(const __grid_constant__ DpBatchParams p) {
     raise_error(p.error, kDevInvalidInput, g);
 }
 
-__global__ void dp_fill_tile_graph_kernel(const __grid_constant__ DpBatchParams p) {
+// Batches issue tickets level-major across graphs (every graph's level-0
+// tiles, then every level-1 tile, ...), so that a tile's children lie far
+// back in the ticket stream; tables and flags stay graph-major.
+__global__ void dp_fill_tile_map_kernel(const __grid_constant__ DpBatchParams p) {
   for (int g = blockIdx.x; g < p.num_graphs; g += gridDim.x) {
     const DpGraph G = p.graphs[g];
-    for (uint32_t t = threadIdx.x; t < G.ntiles; t += blockDim.x)
-      p.tile_graph[G.tile_base + t] = static_cast<uint32_t>(g);
+    uint32_t local = 0;
+    for (int j = 0; j <= G.nh; ++j) {
+      const uint32_t count = p.binom[G.nh][j];
+      const uint32_t base = p.level_base[size_t(g) * (kDpMaxHigh + 2) + j];
+      for (uint32_t i = threadIdx.x; i < count; i += blockDim.x)
+        p.tile_map[base + i] = make_uint2(static_cast<uint32_t>(g), local + i);
+      local += count;
+    }
   }
 }
 
@@ -215,18 +224,22 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   __syncthreads();
 
   for (;;) {
-    uint32_t t = 0, gi = 0;
+    uint32_t t = 0, gi = 0, tl = 0;
     if (lane == 0) {
       t = ld_relaxed_s32(p.error) != 0 ? 0xffffffffu : atomicAdd(p.ticket, 1u);
-      if (t < p.total_tiles && p.graphs)
-        gi = __ldg(p.tile_graph + t);
+      tl = t;
+      if (t < p.total_tiles && p.graphs) {
+        const uint2 m = __ldg(p.tile_map + t);
+        gi = m.x;
+        tl = m.y;
+      }
     }
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= p.total_tiles)
       break;
     gi = __shfl_sync(0xffffffffu, gi, 0);
+    tl = __shfl_sync(0xffffffffu, tl, 0);
     const DpGraph G = p.graphs ? p.graphs[gi] : p.single;
-    const uint32_t tl = t - G.tile_base;
     uint8_t* const table = p.table + G.table_off;
     uint32_t* const flags = p.flags + G.tile_base;
     const uint64_t* const adj = p.adj + G.adj_off;
@@ -372,7 +385,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
     __threadfence();
     __syncwarp();
     if (lane == 0)
-      st_release_u32(p.flags + t, p.epoch);
+      st_release_u32(flags + tl, p.epoch);
   }
 }
 
@@ -595,9 +608,9 @@ cudaError_t dp_launch_validate(const DpBatchParams& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t dp_launch_fill_tile_graph(const DpBatchParams& p, cudaStream_t s) {
+cudaError_t dp_launch_fill_tile_map(const DpBatchParams& p, cudaStream_t s) {
   const int blocks = p.num_graphs < 4096 ? p.num_graphs : 4096;
-  dp_fill_tile_graph_kernel<<<blocks, 256, 0, s>>>(p);
+  dp_fill_tile_map_kernel<<<blocks, 256, 0, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -14,7 +14,7 @@ namespace gtd {
 // real subset and the reconstruction never touches padded vertices.
 struct DpGraph {
   uint64_t table_off = 0;  // byte offset of the graph's table in the table pool
-  uint32_t tile_base = 0;  // first global tile (ticket) of the graph
+  uint32_t tile_base = 0;  // first flag of the graph (graph-major tile count)
   uint32_t ntiles = 0;     // 2^nh
   uint32_t adj_off = 0;    // first adjacency mask; also the first output slot
   int32_t n = 0;           // real vertices
@@ -28,7 +28,8 @@ struct DpBatchParams {
   uint32_t binom[kDpMaxHigh + 1][kDpMaxHigh + 1] = {};  // C(a, b)
   const DpGraph* graphs = nullptr;  // device descriptors; nullptr: only `single`
   DpGraph single;
-  uint32_t* tile_graph = nullptr;   // graph index of every global tile (batches)
+  uint2* tile_map = nullptr;        // ticket -> (graph, local tile) (batches)
+  const uint32_t* level_base = nullptr;  // [graph][level] first ticket (batches)
   int num_graphs = 1;
   int lb = 0;                       // tile bits of this launch
   uint32_t total_tiles = 0;
@@ -50,7 +51,7 @@ struct DpBatchParams {
 void dp_fill_binom(DpBatchParams& p);
 int dp_tile_occupancy(int lb);
 cudaError_t dp_launch_validate(const DpBatchParams& p, cudaStream_t s);
-cudaError_t dp_launch_fill_tile_graph(const DpBatchParams& p, cudaStream_t s);
+cudaError_t dp_launch_fill_tile_map(const DpBatchParams& p, cudaStream_t s);
 cudaError_t dp_launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s);
 cudaError_t dp_launch_tree(const DpBatchParams& p, cudaStream_t s);
 

@@ -51,8 +51,10 @@ struct gtd_handle_s {
   // Batched DP buffers.
   gtd::DpGraph* d_bgraphs = nullptr;
   size_t bgraphs_cap = 0;
-  uint32_t* d_tile_graph = nullptr;
-  size_t tile_graph_cap = 0;
+  uint2* d_tile_map = nullptr;
+  size_t tile_map_cap = 0;
+  uint32_t* d_level_base = nullptr;
+  size_t level_base_cap = 0;
   uint64_t* d_badj = nullptr;
   size_t badj_cap = 0;
   int32_t* d_btd = nullptr;

@@ -164,7 +164,7 @@ gtd_status gtd_dp_solve_batch_device(gtd_handle h, const gtd_graph_desc* descs,
 gtd_status gtd_dp_batch_sync(gtd_handle h, gtd_dp_batch_stats* stats);
 
 /* The autotuner: times the batched DP kernel for every n in [n_min, n_max]
- * and tile bits 8..12 on seeded random graphs (about 2^24 subsets per
+ * and tile bits 8..12 on seeded random graphs (at least 2^26 subsets per
  * measurement) and keeps the rates in the handle; batches solved with
  * tile_bits = 0 then use the tile size with the least predicted time.
  * rates_out (may be NULL) receives (n_max - n_min + 1) x 5 rates in subsets
