@@ -8,7 +8,7 @@ seeded graph generators and text IO (``graphs``) and the build script
 """
 from . import graphs
 from ._lib import GtdError, InvalidArgument, DeadlineExceeded, Handle
-from .treedepth import DynamicGPU, Result
+from .treedepth import BnBGPU, DynamicGPU, Result
 
 __all__ = ["graphs", "GtdError", "InvalidArgument", "DeadlineExceeded", "Handle",
-           "DynamicGPU", "Result"]
+           "DynamicGPU", "BnBGPU", "Result"]

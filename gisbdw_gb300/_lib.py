@@ -264,3 +264,95 @@ def pack_batch(graphs):
 
 def table_index(n: int, tile_bits: int, subset_mask: int) -> int:
     return int(load().gtd_dp_table_index(n, tile_bits, subset_mask))
+
+
+# ---------------------------------------------------------------------------
+# Branch and bound and heuristics.
+# ---------------------------------------------------------------------------
+
+BNB_MAX_N = 104
+
+
+class BnbOpts(ctypes.Structure):
+    _fields_ = [("memo_log2", ctypes.c_int), ("deadline_ns", ctypes.c_uint64), ("ctas_per_sm", ctypes.c_int)]
+
+
+class BnbStats(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_float), ("total_ms", ctypes.c_float), ("nodes", ctypes.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _bind_bnb(L):
+    if getattr(L, "_bnb_bound", False):
+        return L
+    L.gtd_bnb_solve_batch.argtypes = [_vp, _vp, _i, _vp, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                      ctypes.POINTER(BnbOpts), ctypes.POINTER(BnbStats)]
+    L.gtd_heuristic.argtypes = [_vp, _i, _i, _vp, _vp, _vp]
+    L._bnb_bound = True
+    return L
+
+
+def heuristic(g, kind: int = 0, scores=None):
+    """Greedy incumbent (gtd_heuristic): kind 0 HighestDegree(Variance),
+    1 HighestDegree, 2 Variance, 3 highest score first. Host only."""
+    L = _bind_bnb(load())
+    adj = g.adj128()
+    td = ctypes.c_int32()
+    par = np.zeros(g.n, dtype=np.int32)
+    sc = np.ascontiguousarray(scores, dtype=np.float32) if scores is not None else None
+    st = L.gtd_heuristic(_ptr(adj), g.n, kind, _ptr(sc) if sc is not None else None, ctypes.byref(td), _ptr(par))
+    if st != 0:
+        raise _error(st, "gtd_heuristic failed")
+    return td.value, par
+
+
+def pack_bnb(graphs, orders=None, seeds=None, seed_kind: int = 0):
+    """Descriptors, 128-bit adjacency pool, order pool and seeds."""
+    descs = (GraphDesc * len(graphs))()
+    total = sum(g.n for g in graphs)
+    adj = np.zeros(2 * max(total, 1), dtype=np.uint64)
+    order = np.zeros(max(total, 1), dtype=np.uint8)
+    seed_td = np.zeros(len(graphs), dtype=np.int32)
+    seed_par = np.zeros(max(total, 1), dtype=np.int32)
+    off = 0
+    for i, g in enumerate(graphs):
+        descs[i].n = g.n
+        descs[i].offset = off
+        adj[2 * off:2 * (off + g.n)] = g.adj128()
+        order[off:off + g.n] = orders[i] if orders is not None else np.arange(g.n)
+        if seeds is not None:
+            t, p = seeds[i]
+        else:
+            t, p = heuristic(g, seed_kind)
+        seed_td[i] = t
+        seed_par[off:off + g.n] = p
+        off += g.n
+    return descs, adj, order, seed_td, seed_par, total
+
+
+def _bnb_method(self, graphs, orders=None, seeds=None, memo_log2: int = 0, deadline_ns: int = 0,
+                ctas_per_sm: int = 0, packed=None):
+    """Exact treedepth of every graph by the persistent B&B kernel.
+    Returns dict: td, parents, status, proof_ms, nodes, stats."""
+    L = _bind_bnb(self.L)
+    descs, adj, order, seed_td, seed_par, total = packed if packed is not None else pack_bnb(graphs, orders, seeds)
+    count = len(descs)
+    td = np.zeros(count, dtype=np.int32)
+    par = np.zeros(max(total, 1), dtype=np.int32)
+    status = np.zeros(count, dtype=np.int32)
+    proof = np.zeros(count, dtype=np.float32)
+    nodes = np.zeros(count, dtype=np.uint64)
+    opts = BnbOpts(memo_log2, deadline_ns, ctas_per_sm)
+    stats = BnbStats()
+    self._check(L.gtd_bnb_solve_batch(self._h, ctypes.cast(descs, _vp), count, _ptr(adj), total,
+                                      _ptr(order), _ptr(seed_td), _ptr(seed_par), _ptr(td), _ptr(par),
+                                      _ptr(status), _ptr(proof), _ptr(nodes), ctypes.byref(opts),
+                                      ctypes.byref(stats)))
+    parents = [par[d.offset:d.offset + d.n].copy() for d in descs]
+    return {"td": td, "parents": parents, "status": status, "proof_ms": proof, "nodes": nodes,
+            "stats": stats.as_dict(), "seed_td": seed_td}
+
+
+Handle.bnb_solve_batch = _bnb_method

@@ -262,6 +262,7 @@ gtd_status gtd_destroy(gtd_handle h) {
       cudaStreamSynchronize(h->stream);
     if (h->bgraph)
       cudaGraphExecDestroy(h->bgraph);
+    gtd_bnb_release(h);
     cudaFree(h->d_table);
     cudaFree(h->d_flags);
     cudaFree(h->d_io);

@@ -30,6 +30,9 @@ constexpr int kTuneLbMax = 12;
 
 }  // namespace gtd
 
+struct gtd_bnb_state;  // branch-and-bound buffers (gtd_bnb.cu)
+void gtd_bnb_release(struct gtd_handle_s* h);
+
 struct gtd_handle_s {
   int device = 0;
   int num_sms = 0;
@@ -70,6 +73,8 @@ struct gtd_handle_s {
   gtd_dp_batch_stats bstats = {};
   // Autotuner: subsets per millisecond by n and tile bits (0 = unmeasured).
   float tune[GTD_DP_MAX_N + 1][gtd::kTuneLbMax + 1] = {};
+
+  gtd_bnb_state* bnb = nullptr;
 
   // Last DP solve (for gtd_dp_query / gtd_sync).
   bool have_table = false;

@@ -99,3 +99,32 @@ class DynamicGPU:
     def GetTreedepth(self, subset_mask: int) -> int:
         td, _ = self._h.dp_query(subset_mask, want_order=False)
         return td
+
+
+class BnBGPU:
+    """Exact treedepth by the GB300 persistent branch and bound
+    (``td::BnBGPU``, bnb_gpu.hpp:12-17: ``solver(g, heur_td) -> int``).
+    Unlike the reference it also returns the elimination tree
+    (:meth:`Result`). ``order`` is the branching order (vertex tried first
+    at rank 0); by default ascending ids, the reference's DefaultAttemptOrder."""
+
+    def __init__(self, device: int = 0, handle: Optional[_lib.Handle] = None, deadline_ns: int = 0):
+        self._h = handle or _lib.Handle(device)
+        self._deadline = deadline_ns
+        self._res = None
+
+    def __call__(self, g: Graph, heur_td: Optional[int] = None, order=None, seed=None) -> int:
+        if seed is None:
+            seed = _lib.heuristic(g, 0)
+        if heur_td is not None and heur_td < seed[0]:
+            raise _lib.InvalidArgument(1, "heur_td below the seed tree's height needs its tree (pass seed=)")
+        res = self._h.bnb_solve_batch([g], orders=[order] if order is not None else None, seeds=[seed],
+                                      deadline_ns=self._deadline)
+        self._res = res
+        return int(res["td"][0])
+
+    def Result(self) -> Result:
+        if self._res is None:
+            raise _lib.GtdError(7, "no solve yet")
+        par = self._res["parents"][0]
+        return Result(int(self._res["td"][0]), int(np.flatnonzero(par == -1)[0]), par.copy())

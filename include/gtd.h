@@ -172,6 +172,56 @@ gtd_status gtd_dp_batch_sync(gtd_handle h, gtd_dp_batch_stats* stats);
 gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max,
                            float* rates_out);
 
+/* ---- Branch and bound -------------------------------------------------- */
+
+/* Largest n of the branch and bound (memo keys hold 104 vertex bits). */
+#define GTD_BNB_MAX_N 104
+
+typedef struct {
+  int memo_log2;        /* memo slots per graph = 2^memo_log2 (0 = 2^18) */
+  uint64_t deadline_ns; /* per-graph cap on time-to-proof (0 = 120 s) */
+  int ctas_per_sm;      /* 0 = occupancy limit */
+} gtd_bnb_opts;
+
+typedef struct {
+  float ms;             /* device time of search + reconstruction (events) */
+  float total_ms;       /* whole call */
+  uint64_t nodes;       /* search nodes over the batch */
+} gtd_bnb_stats;
+
+/* BranchAndBound (Treedepth/src/branch_and_bound/branch_and_bound.cpp:51-114)
+ * and BnBGPU (bnb_gpu.cu:264-380) over a batch of connected graphs in one
+ * persistent launch: exact treedepth AND an elimination tree per graph (the
+ * reference's GPU B&B returns the treedepth only). Graph i has n = descs[i].n
+ * <= GTD_BNB_MAX_N vertices with 128-bit adjacency masks
+ * adj2_pool[2 (offset + v)] (bits 0-63) and [2 (offset + v) + 1] (bits
+ * 64-127). order_pool[offset + r] is the vertex tried r-th as a root (NULL:
+ * ascending ids, the reference's DefaultAttemptOrder). seed_td[i] and the
+ * tree seed_parent[offset ..] are the incumbent (a heuristic's result, e.g.
+ * gtd_heuristic). Outputs: td_out[i], parent_out[offset ..], status_out[i]
+ * (GTD_OK proven, GTD_TIMEOUT deadline hit: td/tree = best found),
+ * proof_ms_out[i] (time from the launch's first item to the graph's proof)
+ * and nodes_out[i] (search nodes), both optional. Disconnected graphs give
+ * GTD_NOT_CONNECTED and self loops GTD_INVALID_ARG, as the reference's
+ * std::invalid_argument (branch_and_bound.hpp:67-75). */
+gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* descs,
+                               int count, const uint64_t* adj2_pool,
+                               int64_t pool_len, const uint8_t* order_pool,
+                               const int32_t* seed_td,
+                               const int32_t* seed_parent, int32_t* td_out,
+                               int32_t* parent_out, int32_t* status_out,
+                               float* proof_ms_out, uint64_t* nodes_out,
+                               const gtd_bnb_opts* opts, gtd_bnb_stats* stats);
+
+/* Greedy elimination heuristics (host only), the reference's incumbent
+ * seeds (src/branch_and_bound/heuristics/): kind 0 HighestDegree(Variance)
+ * (benchmark.cpp:50-55), 1 HighestDegree, 2 Variance, 3 highest score first
+ * (scores[n] required). adj2 as in gtd_bnb_solve_batch; the graph must be
+ * connected. Writes the tree height and parent array. */
+gtd_status gtd_heuristic(const uint64_t* adj2, int n, int kind,
+                         const float* scores, int32_t* td_out,
+                         int32_t* parent_out);
+
 /* Largest n gtd_dp_solve_noalloc accepts (its fixed scratch holds a 2^n-byte
  * table: 16 MiB at n = 24). */
 #define GTD_DP_NOALLOC_MAX_N 24

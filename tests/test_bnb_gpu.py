@@ -1,0 +1,96 @@
+"""Persistent GPU branch and bound (K2): exact treedepth equal to the subset
+DP's on every graph both can solve, valid elimination trees, the
+reference's own B&B results (fixtures), orders, deadlines, invalid input."""
+import numpy as np
+import pytest
+
+from gisbdw_gb300 import BnBGPU, InvalidArgument, _lib
+from gisbdw_gb300 import graphs as G
+from gisbdw_gb300.validate import check_tree
+
+pytestmark = pytest.mark.gpu
+
+
+CAP_NS = 60 * 10**9  # per-graph cap; every graph here is proven in well under a second
+
+
+def _sparse_c3(count, seed):
+    """Config-3 graphs without the dense G(n, p) members (p up to 0.5 at n up
+    to 24 is the subset DP's territory, not the branch and bound's)."""
+    return [g for g in G.config3_graphs(count=count, seed=seed) if not g.name.startswith("gnp") or g.n <= 16]
+
+
+def _check(handle, gs, **kw):
+    kw.setdefault("deadline_ns", CAP_NS)
+    res = handle.bnb_solve_batch(gs, **kw)
+    assert np.all(res["status"] == 0)
+    for g, t, par in zip(gs, res["td"], res["parents"]):
+        assert check_tree(g, t, par), g.name
+    return res
+
+
+def test_bnb_equals_dp_small_families(handle):
+    gs = [G.path(n) for n in (3, 9, 17)] + [G.cycle(n) for n in (5, 12)] + [G.complete(7), G.star(11)]
+    gs += [G.grid(3, 5), G.grid(4, 4), G.chordal_cycle(14)]
+    gs += _sparse_c3(40, 5)
+    res = _check(handle, gs)
+    dtd, _, _ = handle.dp_solve_batch(gs)
+    assert res["td"].tolist() == dtd.tolist()
+
+
+def test_bnb_equals_dp_random_orders(handle):
+    gs = _sparse_c3(30, 8)
+    rng = np.random.default_rng(1)
+    orders = [rng.permutation(g.n).astype(np.uint8) for g in gs]
+    res = _check(handle, gs, orders=orders)
+    dtd, _, _ = handle.dp_solve_batch(gs)
+    assert res["td"].tolist() == dtd.tolist()
+
+
+def test_bnb_matches_reference_bnb_fixtures(handle, golden):
+    gs, want = [], []
+    for e in golden("ref_solvers.json"):
+        if "bnb_cpu" in e:
+            g = G.Graph(e["n"], [tuple(x) for x in e["edges"]])
+            if g.is_connected():
+                gs.append(g)
+                want.append(e["bnb_cpu"]["td"])
+    res = _check(handle, gs)
+    assert res["td"].tolist() == want
+
+
+def test_bnb_equals_dp_sparse_n28_to_32(handle):
+    gs = [G.sparse_connected(n, s) for n, s in ((28, 1), (30, 2), (32, 3))]
+    gs += [G.grid(5, 6), G.tree_plus_edges(32, 10, 4)]
+    res = _check(handle, gs)
+    for g, t in zip(gs, res["td"]):
+        assert t == handle.dp_solve(g.adj64(), g.n)[0], g.name
+
+
+def test_bnb_class_layer(handle):
+    g = G.gnp_connected(16, 0.3, 2)
+    b = BnBGPU(handle=handle)
+    td = b(g)
+    r = b.Result()
+    assert td == handle.dp_solve(g.adj64(), g.n)[0]
+    assert check_tree(g, td, r.parent) and r.parent[r.root] == -1
+
+
+def test_bnb_invalid_inputs(handle):
+    with pytest.raises(InvalidArgument):
+        handle.bnb_solve_batch([G.Graph(4, [(0, 1), (2, 3)])], seeds=[(2, np.array([-1, 0, -1, 2]))])
+    g = G.path(4)
+    descs, adj, order, st, sp, total = _lib.pack_bnb([g])
+    adj[2 * 1] |= np.uint64(1 << 1)
+    with pytest.raises(InvalidArgument):
+        handle.bnb_solve_batch([g], packed=(descs, adj, order, st, sp, total))
+
+
+def test_bnb_deadline_reports_timeout_and_stays_usable(handle):
+    gs = G.config4_graphs(count=3)
+    res = handle.bnb_solve_batch(gs, deadline_ns=1000)
+    assert set(res["status"].tolist()) <= {0, 4}
+    for g, t, par in zip(gs, res["td"], res["parents"]):
+        assert check_tree(g, t, par)  # best found so far is still a valid tree
+    r2 = _check(handle, [G.cycle(9)])
+    assert r2["td"][0] == 5
