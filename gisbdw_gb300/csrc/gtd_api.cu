@@ -273,6 +273,7 @@ gtd_status gtd_destroy(gtd_handle h) {
     cudaFree(h->d_badj);
     cudaFree(h->d_btd);
     cudaFree(h->d_bparent);
+    cudaFree(h->d_scratch);
     if (h->h_pinned)
       cudaFreeHost(h->h_pinned);
     if (h->h_bstage)
@@ -426,6 +427,34 @@ gtd_status gtd_dp_read_table(gtd_handle h, uint8_t* out, uint64_t bytes) {
     return fail(h, GTD_INVALID_ARG, "output buffer smaller than the table");
   DeviceGuard g(h->device);
   GTD_CUDA(h, cudaMemcpyAsync(out, h->d_table, need, cudaMemcpyDeviceToHost, h->stream));
+  GTD_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GTD_OK;
+}
+
+gtd_status gtd_dp_labels(gtd_handle h, const uint64_t* subsets, int count, int32_t* td_out,
+                         uint64_t* roots_out) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!h->have_table)
+    return fail(h, GTD_NO_RESULT, "no DP table: solve a graph first");
+  if (!subsets || !td_out || !roots_out || count < 0)
+    return fail(h, GTD_INVALID_ARG, "null pointer argument");
+  if (count == 0)
+    return GTD_OK;
+  const int n = h->last_params.single.n;
+  for (int i = 0; i < count; ++i)
+    if (n < 64 && (subsets[i] >> n))
+      return fail(h, GTD_INVALID_ARG, "subset has a vertex >= n");
+  DeviceGuard g(h->device);
+  const size_t bytes = size_t(count) * (2 * sizeof(uint64_t) + sizeof(int32_t));
+  GTD_CUDA(h, ensure_device(&h->d_scratch, &h->scratch_cap, bytes));
+  uint64_t* d_sub = static_cast<uint64_t*>(h->d_scratch);
+  uint64_t* d_roots = d_sub + count;
+  int32_t* d_td = reinterpret_cast<int32_t*>(d_roots + count);
+  GTD_CUDA(h, cudaMemcpyAsync(d_sub, subsets, count * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+  GTD_CUDA(h, dp_launch_labels(h->last_params, d_sub, count, d_td, d_roots, h->stream));
+  GTD_CUDA(h, cudaMemcpyAsync(td_out, d_td, count * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  GTD_CUDA(h, cudaMemcpyAsync(roots_out, d_roots, count * sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream));
   GTD_CUDA(h, cudaStreamSynchronize(h->stream));
   return GTD_OK;
 }

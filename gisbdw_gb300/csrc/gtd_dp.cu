@@ -635,4 +635,47 @@ cudaError_t dp_launch_tree(const DpBatchParams& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Training labels from a solved table (single graph): for each subset S,
+// td(S) and, when S is connected, its optimal-root set
+// R(S) = {v in S : td(S - v) = td(S) - 1} (one warp per subset).
+__global__ void __launch_bounds__(32 * kTreeWarps)
+    dp_labels_kernel(const __grid_constant__ DpBatchParams p, const uint64_t* subsets, int count, int32_t* td_out,
+                     uint64_t* roots_out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const DpGraph G = p.single;
+  const TreeCtx ctx{p.binom, p.table + G.table_off, p.lb, G.nh, G.n};
+  for (int i = blockIdx.x * kTreeWarps + warp; i < count; i += gridDim.x * kTreeWarps) {
+    const uint64_t S = subsets[i];
+    if (S == 0) {
+      if (lane == 0) {
+        td_out[i] = 0;
+        roots_out[i] = 0;
+      }
+      continue;
+    }
+    const uint32_t td = ctx.td_of(S);
+    bool lo = false, hi = false;
+    if ((S >> lane) & 1ull)
+      lo = ctx.td_of(S & ~(1ull << lane)) + 1u == td;
+    if (lane + 32 < G.n && ((S >> (lane + 32)) & 1ull))
+      hi = ctx.td_of(S & ~(1ull << (lane + 32))) + 1u == td;
+    const uint64_t roots = ballot64(lo, hi);
+    if (lane == 0) {
+      td_out[i] = static_cast<int32_t>(td);
+      roots_out[i] = roots;
+    }
+  }
+}
+
+cudaError_t dp_launch_labels(const DpBatchParams& p, const uint64_t* subsets, int count, int32_t* td_out,
+                             uint64_t* roots_out, cudaStream_t s) {
+  int blocks = (count + kTreeWarps - 1) / kTreeWarps;
+  if (blocks > 8192)
+    blocks = 8192;
+  if (blocks < 1)
+    blocks = 1;
+  dp_labels_kernel<<<blocks, 32 * kTreeWarps, 0, s>>>(p, subsets, count, td_out, roots_out);
+  return cudaGetLastError();
+}
+
 }  // namespace gtd

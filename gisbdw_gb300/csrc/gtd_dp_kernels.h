@@ -54,5 +54,7 @@ cudaError_t dp_launch_validate(const DpBatchParams& p, cudaStream_t s);
 cudaError_t dp_launch_fill_tile_map(const DpBatchParams& p, cudaStream_t s);
 cudaError_t dp_launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s);
 cudaError_t dp_launch_tree(const DpBatchParams& p, cudaStream_t s);
+cudaError_t dp_launch_labels(const DpBatchParams& p, const uint64_t* subsets, int count, int32_t* td_out,
+                             uint64_t* roots_out, cudaStream_t s);
 
 }  // namespace gtd

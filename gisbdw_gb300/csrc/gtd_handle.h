@@ -75,6 +75,8 @@ struct gtd_handle_s {
   float tune[GTD_DP_MAX_N + 1][gtd::kTuneLbMax + 1] = {};
 
   gtd_bnb_state* bnb = nullptr;
+  void* d_scratch = nullptr;  // general device scratch (labels, GNN batches)
+  size_t scratch_cap = 0;
 
   // Last DP solve (for gtd_dp_query / gtd_sync).
   bool have_table = false;

@@ -222,6 +222,56 @@ gtd_status gtd_heuristic(const uint64_t* adj2, int n, int kind,
                          const float* scores, int32_t* td_out,
                          int32_t* parent_out);
 
+/* Training labels from the last single-graph DP solve: for subsets[i], its
+ * treedepth td_out[i] and, when the subset is connected, the mask of its
+ * optimal roots roots_out[i] (v with td(S - v) = td(S) - 1, the root set every
+ * reference DP chooses from, dynamic_cpu.cpp:96-99). */
+gtd_status gtd_dp_labels(gtd_handle h, const uint64_t* subsets, int count,
+                         int32_t* td_out, uint64_t* roots_out);
+
+/* ---- Learned branching order (no counterpart in the reference) --------- */
+
+/* A message-passing GNN (input projection, `layers` mean-aggregation layers
+ * of width `hidden` <= 64, ReLU) with a per-vertex root logit and a
+ * per-graph treedepth estimate; BF16 weights, FP32 accumulation, own
+ * forward / backward / Adam kernels. It orders the branch and bound's
+ * candidates and seeds its incumbent; it never prunes. */
+typedef struct gtd_gnn_s* gtd_gnn;
+
+/* One batch of graphs: nodes of graph g are [graph_start[g],
+ * graph_start[g + 1]); node v's neighbours (batch indices) are
+ * nbr[nbr_start[v] .. nbr_start[v + 1]); x holds num_nodes x in_features
+ * features. Labels (training only): root_label / node_mask per node (loss
+ * over nodes with mask 1), td_label per graph. */
+typedef struct {
+  int num_nodes;
+  int num_graphs;
+  const float* x;
+  const int32_t* graph_start;
+  const int32_t* nbr_start;
+  const int32_t* nbr;
+  const float* root_label;
+  const float* node_mask;
+  const float* td_label;
+} gtd_gnn_batch;
+
+gtd_status gtd_gnn_create(gtd_handle h, int in_features, int hidden,
+                          int layers, uint64_t seed, gtd_gnn* out);
+gtd_status gtd_gnn_destroy(gtd_gnn g);
+int64_t gtd_gnn_num_params(gtd_gnn g);
+/* FP32 master parameters (the BF16 weights are their rounding). */
+gtd_status gtd_gnn_get_params(gtd_gnn g, float* out);
+gtd_status gtd_gnn_set_params(gtd_gnn g, const float* in);
+gtd_status gtd_gnn_forward(gtd_gnn g, const gtd_gnn_batch* b,
+                           float* logits_out, float* td_out);
+/* Loss and its gradient w.r.t. every parameter (for checks). */
+gtd_status gtd_gnn_gradients(gtd_gnn g, const gtd_gnn_batch* b,
+                             float td_weight, float* grad_out,
+                             float* loss_out);
+/* One Adam step (lr, betas 0.9 / 0.999) on the batch's loss. */
+gtd_status gtd_gnn_train_step(gtd_gnn g, const gtd_gnn_batch* b, float lr,
+                              float td_weight, float* loss_out);
+
 /* Largest n gtd_dp_solve_noalloc accepts (its fixed scratch holds a 2^n-byte
  * table: 16 MiB at n = 24). */
 #define GTD_DP_NOALLOC_MAX_N 24
