@@ -35,8 +35,10 @@
 //    every item below is cancelled. A graph is proven when the lower bound
 //    meets the best. Running items re-check this (and a per-graph deadline
 //    on %globaltimer) every 64 nodes and stop early.
-//  * Reconstruction: one warp per graph re-decides, below the best root,
-//    every component at the depth it needs (memo hits).
+//  * Trees: the first success of a level builds its elimination tree at
+//    once (re-deciding each component at the depth it needs: memo hits)
+//    into a per-level buffer, and only then publishes the level; the final
+//    kernel copies the best level's tree (or the seed's) out.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -81,6 +83,8 @@ struct BnbParams {
   uint32_t* best = nullptr;        // per graph: k << 8 | root (kSeedRoot = seed tree)
   uint32_t* lbp = nullptr;         // per graph: proven lower bound
   uint32_t* fails = nullptr;       // per graph x level: failed candidates
+  uint32_t* claim = nullptr;       // per graph x level: tree buffer taken
+  int8_t* lvl_parent = nullptr;    // per graph x level: tree (max_n entries, -1 root)
   int32_t* status = nullptr;       // per graph BnbStatus
   uint64_t* t_begin = nullptr;     // per graph: first item start (globaltimer ns)
   unsigned long long* t_end = nullptr;  // per graph: proof time
@@ -107,6 +111,8 @@ struct WarpMem {
   uint64_t wlo[kBnbMaxN], whi[kBnbMaxN];   // contraction work copy (minor-min-width)
   uint64_t slo[kMaxComps], shi[kMaxComps]; // components of C - v with >= 3 vertices
   Frame fr[kBnbMaxN + 2];
+  uint64_t qlo[kBnbMaxN], qhi[kBnbMaxN];   // tree building: components still to root
+  uint8_t qown[kBnbMaxN], qk[kBnbMaxN], qdep[kBnbMaxN];
   uint8_t ssz[kMaxComps];
   uint8_t order[kBnbMaxN];
 };
@@ -202,14 +208,21 @@ __device__ void memo_put(uint4* table, uint32_t mask, uint64_t lo, uint64_t hi, 
     return hi | (static_cast<uint64_t>(nlb & 0x7F) << 40) | (static_cast<uint64_t>(nub & 0x7F) << 47) |
            (static_cast<uint64_t>(nroot & 0x7F) << 54);
   };
+  int victim = 0, victim_size = 1 << 30;
   for (int p = 0; p < kMemoProbes; ++p) {
     uint4* slot = table + ((h + p) & mask);
     uint64_t clo = 0, chi = 0;
     cas128(slot, 0, 0, 0, 0, clo, chi);
     for (int tries = 0; tries < 64; ++tries) {
       const bool empty = clo == 0 && chi == 0;
-      if (!empty && !(clo == lo && (chi & kKeyHiMask) == hi))
+      if (!empty && !(clo == lo && (chi & kKeyHiMask) == hi)) {
+        const int sz = __popcll(clo) + __popcll(chi & kKeyHiMask);
+        if (sz < victim_size) {
+          victim_size = sz;
+          victim = p;
+        }
         break;  // another key: next probe
+      }
       const uint64_t nhi = merged(chi, empty);
       if (!empty && nhi == chi)
         return;
@@ -221,8 +234,9 @@ __device__ void memo_put(uint4* table, uint32_t mask, uint64_t lo, uint64_t hi, 
       chi = ohi;
     }
   }
-  // every probe holds another key: overwrite the first (the memo is a cache)
-  uint4* slot = table + (h & mask);
+  // every probe holds another key: the memo is a cache, so overwrite the
+  // entry of the smallest component (the cheapest to decide again)
+  uint4* slot = table + ((h + victim) & mask);
   uint64_t clo = 0, chi = 0;
   cas128(slot, 0, 0, 0, 0, clo, chi);
   for (int tries = 0; tries < 64; ++tries) {
@@ -621,6 +635,63 @@ struct Search {
       *root_out = ret_root;
     return ret && !timed_out && !cancelled;
   }
+
+  // Elimination tree of C (depth <= k) below the accepted root: every
+  // component left is decided again at the depth it needs, which the memo
+  // entries written by the accepting search answer at once (a search only
+  // where an entry has been evicted). parent_out[u] (int8, -1 at the root)
+  // for u in C. False if a component fails (an error), or on a stop.
+  __device__ bool build_tree(uint64_t Clo, uint64_t Chi, int k, int root, int8_t* parent_out) {
+    if (lane == 0)
+      parent_out[root] = -1;
+    int top = 0;
+    uint64_t rlo = Clo, rhi = Chi;
+    bit_clear(rlo, rhi, root);
+    while (rlo | rhi) {
+      uint64_t clo, chi;
+      component(rlo, rhi, first128(rlo, rhi), clo, chi);
+      rlo &= ~clo;
+      rhi &= ~chi;
+      if (lane == 0) {
+        w->qlo[top] = clo;
+        w->qhi[top] = chi;
+        w->qown[top] = static_cast<uint8_t>(root);
+        w->qk[top] = static_cast<uint8_t>(k - 1);
+        w->qdep[top] = 2;
+      }
+      ++top;
+    }
+    __syncwarp();
+    while (top > 0) {
+      --top;
+      const uint64_t clo = w->qlo[top], chi = w->qhi[top];
+      const int owner = w->qown[top], kk = w->qk[top], depth = w->qdep[top];
+      __syncwarp();
+      int r = -1;
+      if (depth > k || !decide(clo, chi, kk, -1, &r) || r < 0)
+        return false;
+      if (lane == 0)
+        parent_out[r] = static_cast<int8_t>(owner);
+      uint64_t xlo = clo, xhi = chi;
+      bit_clear(xlo, xhi, r);
+      while (xlo | xhi) {
+        uint64_t dlo, dhi;
+        component(xlo, xhi, first128(xlo, xhi), dlo, dhi);
+        xlo &= ~dlo;
+        xhi &= ~dhi;
+        if (lane == 0) {
+          w->qlo[top] = dlo;
+          w->qhi[top] = dhi;
+          w->qown[top] = static_cast<uint8_t>(r);
+          w->qk[top] = static_cast<uint8_t>(kk - 1);
+          w->qdep[top] = static_cast<uint8_t>(depth + 1);
+        }
+        ++top;
+      }
+      __syncwarp();
+    }
+    return true;
+  }
 };
 
 __device__ void load_graph(WarpMem* w, const BnbParams& p, const BnbGraph& G, int lane) {
@@ -699,13 +770,32 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
     const bool pendant = G.n >= 3 && s.deg_in(v, fl, fh) == 1;  // dominated by its neighbour
     if (!pendant)
       ok = s.decide(fl, fh, k, v, nullptr);
+    // A success is published only with its tree: the first success of a
+    // level claims the level's parent buffer and builds the tree while the
+    // memo entries of its search are fresh; later successes of the level
+    // are redundant.
+    bool publish = false;
+    if (ok) {
+      int claimed = 0;
+      if (lane == 0)
+        claimed = atomicCAS(p.claim + size_t(g) * p.levels + li, 0u, 1u) == 0u;
+      claimed = __shfl_sync(0xffffffffu, claimed, 0);
+      if (claimed) {
+        int8_t* tree = p.lvl_parent + (size_t(g) * p.levels + li) * p.max_n;
+        publish = s.build_tree(fl, fh, k, v, tree);
+        if (!publish && !s.timed_out && !s.cancelled && lane == 0)
+          raise_error(p.error, kDevNoRoot, g);
+        __threadfence();
+      }
+    }
     if (lane == 0) {
       atomicAdd(p.nodes + g, s.nodes);
       if (s.timed_out) {
         atomicExch(p.status + g, kBnbTimeout);
       } else if (!s.cancelled) {
         if (ok) {
-          atomicMin(p.best + g, (static_cast<uint32_t>(k) << 8) | static_cast<uint32_t>(v));
+          if (publish)
+            atomicMin(p.best + g, (static_cast<uint32_t>(k) << 8) | static_cast<uint32_t>(v));
         } else if (atomicAdd(p.fails + size_t(g) * p.levels + li, 1u) + 1 == static_cast<uint32_t>(G.n)) {
           atomicMax(p.lbp + g, static_cast<uint32_t>(k + 1));  // every root failed: td > k
         }
@@ -716,13 +806,9 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
   }
 }
 
-// One warp per graph: the final tree below the best root.
-__global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_tree_kernel(const __grid_constant__ BnbParams p) {
-  extern __shared__ __align__(16) uint8_t smem[];
+// One warp per graph: td and tree of the best level (or the seed's).
+__global__ void bnb_tree_kernel(const __grid_constant__ BnbParams p) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpMem* w = reinterpret_cast<WarpMem*>(smem) + warp;
-  __shared__ uint64_t qlo[kBnbWarps][kBnbMaxN], qhi[kBnbWarps][kBnbMaxN];
-  __shared__ int32_t qown[kBnbWarps][kBnbMaxN], qk[kBnbWarps][kBnbMaxN], qdepth[kBnbWarps][kBnbMaxN];
   for (int g = blockIdx.x * kBnbWarps + warp; g < p.num_graphs; g += gridDim.x * kBnbWarps) {
     const BnbGraph G = p.graphs[g];
     int32_t* parent = p.parent_out + G.adj_off;
@@ -735,64 +821,10 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_tree_kernel(const __gri
         parent[v] = p.seed_parent[G.adj_off + v];
       continue;
     }
-    load_graph(w, p, G, lane);
-    Search s{w, lane, G.n, p.memo + G.memo_off, p.memo_mask, StopCheck{}, 0ull, false, false};
-    uint64_t fl, fh;
-    full_set(G.n, fl, fh);
-    if (lane == 0)
-      parent[root] = -1;
-    int top = 0, height = 1;
-    uint64_t rlo = fl, rhi = fh;
-    bit_clear(rlo, rhi, root);
-    while (rlo | rhi) {
-      uint64_t clo, chi;
-      s.component(rlo, rhi, first128(rlo, rhi), clo, chi);
-      rlo &= ~clo;
-      rhi &= ~chi;
-      if (lane == 0) {
-        qlo[warp][top] = clo;
-        qhi[warp][top] = chi;
-        qown[warp][top] = root;
-        qk[warp][top] = td - 1;
-        qdepth[warp][top] = 2;
-      }
-      ++top;
-    }
-    __syncwarp();
-    bool bad = false;
-    while (top > 0 && !bad) {
-      --top;
-      const uint64_t clo = qlo[warp][top], chi = qhi[warp][top];
-      const int owner = qown[warp][top], kk = qk[warp][top], depth = qdepth[warp][top];
-      __syncwarp();
-      int r = -1;
-      if (!s.decide(clo, chi, kk, -1, &r) || r < 0) {
-        bad = true;
-        break;
-      }
-      if (lane == 0)
-        parent[r] = owner;
-      height = max(height, depth);
-      uint64_t xlo = clo, xhi = chi;
-      bit_clear(xlo, xhi, r);
-      while (xlo | xhi) {
-        uint64_t dlo, dhi;
-        s.component(xlo, xhi, first128(xlo, xhi), dlo, dhi);
-        xlo &= ~dlo;
-        xhi &= ~dhi;
-        if (lane == 0) {
-          qlo[warp][top] = dlo;
-          qhi[warp][top] = dhi;
-          qown[warp][top] = r;
-          qk[warp][top] = kk - 1;
-          qdepth[warp][top] = depth + 1;
-        }
-        ++top;
-      }
-      __syncwarp();
-    }
-    if ((bad || height > td) && lane == 0)
-      raise_error(p.error, kDevNoRoot, g);
+    const int li = G.ub0 - 1 - td;
+    const int8_t* tree = p.lvl_parent + (size_t(g) * p.levels + li) * p.max_n;
+    for (int v = lane; v < G.n; v += 32)
+      parent[v] = tree[v];
   }
 }
 
@@ -919,6 +951,8 @@ struct gtd_bnb_state {
   size_t u32_cap = 0;
   uint64_t* u64 = nullptr; // t_begin, t_end, nodes, t0
   size_t u64_cap = 0;
+  int8_t* i8 = nullptr;    // per-level trees
+  size_t i8_cap = 0;
 };
 
 void gtd_bnb_release(gtd_handle h) {
@@ -932,6 +966,7 @@ void gtd_bnb_release(gtd_handle h) {
   cudaFree(b->i32);
   cudaFree(b->u32);
   cudaFree(b->u64);
+  cudaFree(b->i8);
   delete b;
   h->bnb = nullptr;
 }
@@ -962,7 +997,18 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   if (!h->bnb)
     h->bnb = new gtd_bnb_state();
   gtd_bnb_state& B = *h->bnb;
-  const int memo_log2 = (opts && opts->memo_log2 > 0) ? std::min(opts->memo_log2, 26) : 18;
+  int memo_log2 = (opts && opts->memo_log2 > 0) ? std::min(opts->memo_log2, 26) : 0;
+  if (memo_log2 == 0) {
+    // HBM is the memo: up to a quarter of the free memory (at most 32 GiB),
+    // 2^16 .. 2^24 slots of 16 bytes per graph
+    size_t free_b = 0, total_b = 0;
+    GTD_CUDA(h, cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = std::min(free_b / 4 + B.memo_cap * sizeof(uint4), size_t(32) << 30);
+    const size_t per_graph = budget / sizeof(uint4) / size_t(count);
+    memo_log2 = 16;
+    while (memo_log2 < 24 && (size_t(1) << (memo_log2 + 1)) <= per_graph)
+      ++memo_log2;
+  }
   const size_t slots = size_t(1) << memo_log2;
 
   std::vector<BnbGraph> graphs(count);
@@ -1006,7 +1052,8 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   if ((s = grow(h, &B.order, &B.order_cap, size_t(pool_len) + 16)) != GTD_OK) return s;
   if ((s = grow(h, &B.memo, &B.memo_cap, slots * count)) != GTD_OK) return s;
   if ((s = grow(h, &B.i32, &B.i32_cap, 2 * size_t(pool_len) + 2 * size_t(count))) != GTD_OK) return s;
-  if ((s = grow(h, &B.u32, &B.u32_cap, size_t(count) * (2 + levels))) != GTD_OK) return s;
+  if ((s = grow(h, &B.u32, &B.u32_cap, size_t(count) * (2 + 2 * size_t(levels)))) != GTD_OK) return s;
+  if ((s = grow(h, &B.i8, &B.i8_cap, size_t(count) * levels * max_n)) != GTD_OK) return s;
   if ((s = grow(h, &B.u64, &B.u64_cap, 3 * size_t(count) + 1)) != GTD_OK) return s;
   int32_t* d_seed_parent = B.i32;
   int32_t* d_parent = B.i32 + pool_len;
@@ -1015,6 +1062,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   uint32_t* d_best = B.u32;
   uint32_t* d_lbp = B.u32 + count;
   uint32_t* d_fails = B.u32 + 2 * count;
+  uint32_t* d_claim = d_fails + size_t(count) * levels;
   uint64_t* d_tbeg = B.u64;
   uint64_t* d_tend = B.u64 + count;
   uint64_t* d_nodes = B.u64 + 2 * count;
@@ -1029,7 +1077,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
                               h->stream));
   GTD_CUDA(h, cudaMemcpyAsync(d_best, best.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   GTD_CUDA(h, cudaMemcpyAsync(d_lbp, lbp.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-  GTD_CUDA(h, cudaMemsetAsync(d_fails, 0, size_t(count) * levels * sizeof(uint32_t), h->stream));
+  GTD_CUDA(h, cudaMemsetAsync(d_fails, 0, 2 * size_t(count) * levels * sizeof(uint32_t), h->stream));
   GTD_CUDA(h, cudaMemsetAsync(B.memo, 0, slots * count * sizeof(uint4), h->stream));
   GTD_CUDA(h, cudaMemsetAsync(d_status, 0, count * sizeof(int32_t), h->stream));
   GTD_CUDA(h, cudaMemsetAsync(B.u64, 0, 3 * size_t(count) * sizeof(uint64_t), h->stream));
@@ -1048,6 +1096,8 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   p.best = d_best;
   p.lbp = d_lbp;
   p.fails = d_fails;
+  p.claim = d_claim;
+  p.lvl_parent = B.i8;
   p.status = d_status;
   p.t_begin = d_tbeg;
   p.t_end = reinterpret_cast<unsigned long long*>(d_tend);
@@ -1062,8 +1112,6 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
 
   const size_t smem = sizeof(WarpMem) * kBnbWarps;
   GTD_CUDA(h, cudaFuncSetAttribute(bnb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  GTD_CUDA(h, cudaFuncSetAttribute(bnb_tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem)));
   int occ = 0;
   GTD_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bnb_kernel, 32 * kBnbWarps, smem));
   if (opts && opts->ctas_per_sm > 0 && opts->ctas_per_sm < occ)
@@ -1077,7 +1125,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   bnb_kernel<<<static_cast<int>(ctas), 32 * kBnbWarps, smem, h->stream>>>(p);
   GTD_CUDA(h, cudaGetLastError());
   const int tree_ctas = std::min(4096, (count + kBnbWarps - 1) / kBnbWarps);
-  bnb_tree_kernel<<<tree_ctas, 32 * kBnbWarps, smem, h->stream>>>(p);
+  bnb_tree_kernel<<<tree_ctas, 32 * kBnbWarps, 0, h->stream>>>(p);
   GTD_CUDA(h, cudaGetLastError());
   GTD_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
 

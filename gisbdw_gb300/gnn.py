@@ -384,7 +384,7 @@ def root_accuracy(net: GNN, samples) -> dict:
             rand += y.mean()
             td_err.append(abs(float(td[k]) - t))
     n = max(1, len(samples))
-    return {"top1_root": hits / n, "max_degree_root": deg_hits / n, "uniform_root": rand / n,
+    return {"top1_root": float(hits) / n, "max_degree_root": float(deg_hits) / n, "uniform_root": float(rand) / n,
             "td_mae": float(np.mean(td_err)) if td_err else None, "samples": len(samples)}
 
 

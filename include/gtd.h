@@ -178,7 +178,7 @@ gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max,
 #define GTD_BNB_MAX_N 104
 
 typedef struct {
-  int memo_log2;        /* memo slots per graph = 2^memo_log2 (0 = 2^18) */
+  int memo_log2;        /* memo slots per graph = 2^memo_log2 (0 = sized from free HBM, 2^16..2^24) */
   uint64_t deadline_ns; /* per-graph cap on time-to-proof (0 = 120 s) */
   int ctas_per_sm;      /* 0 = occupancy limit */
 } gtd_bnb_opts;

