@@ -6,6 +6,17 @@ Workload (default, ``--workload dp-c2``): the single-graph subset DP at scale,
 elimination tree). The DP tables (256 MiB - 4 GiB) are larger than L2, so no
 flush is needed between steps.
 
+The same line carries two more measurements of the run:
+  dp_c3   batched uneven DP, 4096 graphs n in [10, 24] (three families), one
+          persistent launch per step replayed from a CUDA graph;
+  bnb_c4  plain vs learned-guided GPU branch and bound on 256 sparse graphs
+          n in [40, 64] (random geometric, random 3-regular, deleted grids)
+          with a per-graph cap: plain = ascending candidate order (the
+          reference's DefaultAttemptOrder) and the reference heuristic's
+          incumbent; learned = the GNN's score order and the better of that
+          incumbent and a score-greedy elimination. The GNN is trained in the
+          run, on the GPU, from labels the GPU DP computes.
+
 Arms:
   default            gtd on the GPU; ``value`` = solves/s with inputs resident
                      on the device; ``e2e`` = the same through the host-buffer
@@ -48,6 +59,14 @@ def parse_args():
                     help="restrict the workload to its graphs with this n (profiling)")
     ap.add_argument("--tile-bits", type=int, default=0,
                     help="DP tile bits (0 = the library's default)")
+    ap.add_argument("--no-c3", action="store_true", help="skip the batched DP measurement")
+    ap.add_argument("--no-bnb", action="store_true", help="skip the plain vs learned B&B measurement")
+    ap.add_argument("--bnb-graphs", type=int, default=256, help="B&B graphs (config 4 family)")
+    ap.add_argument("--bnb-cap-s", type=float, default=10.0, help="B&B per-graph cap on time to proof")
+    ap.add_argument("--bnb-memo-log2", type=int, default=0,
+                    help="B&B memo slots per graph as a power of two (0 = sized from free HBM)")
+    ap.add_argument("--label-graphs", type=int, default=1500,
+                    help="graphs (n in [10, 24]) whose DP tables label the GNN training set")
     return ap.parse_args()
 
 
@@ -190,6 +209,85 @@ def run_reference(args, graphs):
 # GPU arm.
 # ---------------------------------------------------------------------------
 
+def measure_dp_c3(h, steps, warmup):
+    """Batched uneven DP on config 3 (4096 graphs), device time from the
+    library's events and host time of the whole C-ABI call."""
+    from gisbdw_gb300 import _lib
+    from gisbdw_gb300 import graphs as G
+    from gisbdw_gb300.validate import check_tree
+    graphs = G.config3_graphs()
+    packed = _lib.pack_batch(graphs)
+    for _ in range(warmup):
+        td, pars, st = h.dp_solve_batch(graphs, packed=packed)
+    bad = [g.name for g, t, p in zip(graphs[::64], td[::64], pars[::64]) if not check_tree(g, int(t), p)]
+    dev, host = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        td, pars, st = h.dp_solve_batch(graphs, packed=packed)
+        host.append(time.perf_counter() - t0)
+        dev.append(st["dp_ms"])
+    peak, peak_kind = peaks()
+    ms = statistics.median(dev)
+    return {"graphs": len(graphs), "solves_per_s": len(graphs) / (ms / 1e3), "dp_ms": ms,
+            "e2e_solves_per_s": len(graphs) / statistics.median(host), "alg_bytes": st["alg_bytes"],
+            "alg_GBps": st["alg_bytes"] / (ms / 1e3) / 1e9, "frac_of_" + peak_kind + "_hbm":
+            st["alg_bytes"] / (ms / 1e3) / 1e9 / peak, "tile_bits": st["tile_bits"], "ctas": st["ctas"],
+            "cuda_graph_replayed": bool(st["graph_replayed"]), "trees_checked": len(graphs[::64]),
+            "trees_invalid": bad}
+
+
+def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0):
+    """Plain vs learned-guided B&B on the config 4 family (identical graphs),
+    the GNN trained here on DP labels."""
+    import numpy as np
+    from gisbdw_gb300 import gnn
+    from gisbdw_gb300 import graphs as G
+    from gisbdw_gb300.validate import check_tree
+    t0 = time.perf_counter()
+    samples = gnn.label_samples(h, G.config3_graphs(count=n_label, seed=11), per_graph=20, seed=1)
+    t1 = time.perf_counter()
+    cut = len(samples) * 9 // 10
+    net = gnn.GNN(h, seed=1)
+    losses = gnn.train(net, samples[:cut], epochs=8, batch_graphs=256, lr=3e-3)
+    t2 = time.perf_counter()
+    acc = gnn.root_accuracy(net, samples[cut:])
+    graphs = G.config4_graphs(count=n_graphs)
+    cap_ns = int(cap_s * 1e9)
+    h.bnb_solve_batch(graphs[:4], deadline_ns=10**8, memo_log2=memo_log2)  # warm-up (allocation, module load)
+    plain = h.bnb_solve_batch(graphs, deadline_ns=cap_ns, memo_log2=memo_log2)
+    t3 = time.perf_counter()
+    orders, seeds = gnn.orders_and_seeds(net, graphs)
+    t_inf = time.perf_counter() - t3
+    learned = h.bnb_solve_batch(graphs, orders=orders, seeds=seeds, deadline_ns=cap_ns, memo_log2=memo_log2)
+
+    def summary(res, extra_s=0.0):
+        ok = res["status"] == 0
+        pm = res["proof_ms"]
+        fam = {}
+        for f in ("rgg", "reg3", "grid"):
+            sel = np.array([g.name.startswith(f) for g in graphs])
+            fam[f] = f"{int((ok & sel).sum())}/{int(sel.sum())}"
+        return {"solved": int(ok.sum()), "solves_per_s": float(ok.sum() / (res["stats"]["ms"] / 1e3)),
+                "e2e_solves_per_s": float(ok.sum() / (res["stats"]["total_ms"] / 1e3 + extra_s)),
+                "p50_proof_ms_solved": float(np.median(pm[ok])) if ok.any() else None,
+                "p50_proof_ms_capped": float(np.median(np.where(ok, pm, cap_s * 1e3))),
+                "p99_proof_ms_capped": float(np.percentile(np.where(ok, pm, cap_s * 1e3), 99)),
+                "nodes": int(res["nodes"].sum()), "batch_ms": res["stats"]["ms"], "by_family": fam,
+                "trees_valid": all(check_tree(g, int(t), par) for g, t, par in
+                                   zip(graphs, res["td"], res["parents"]))}
+    ps, ls = summary(plain), summary(learned, t_inf)
+    both = (plain["status"] == 0) & (learned["status"] == 0)
+    out = {"graphs": len(graphs), "cap_s": cap_s, "plain": ps, "learned": ls, "both_solved": int(both.sum()),
+           "td_identical_on_both": bool(np.array_equal(plain["td"][both], learned["td"][both])),
+           "gnn": {"labels": len(samples), "label_s": t1 - t0, "train_s": t2 - t1, "train_steps": len(losses),
+                   "held_out": acc, "inference_s": t_inf, "layers": gnn.LAYERS, "hidden": gnn.HIDDEN,
+                   "weights": "bf16 (fp32 master, fp32 accumulation)"}}
+    if both.any():
+        pp, lp = np.median(plain["proof_ms"][both]), np.median(learned["proof_ms"][both])
+        out["p50_proof_ms_both"] = {"plain": float(pp), "learned": float(lp), "plain_over_learned": float(pp / lp)}
+    return out
+
+
 def run_gpu(args, graphs):
     import numpy as np
     import torch
@@ -304,9 +402,13 @@ def run_gpu(args, graphs):
                      "launch_ms_mean": kms / launches, "by_n": by_n_out},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": 2 * launches,
+        "gpu_launches": 3 * launches,
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_c3:
+        line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup)
+    if rank == 0 and not args.no_bnb:
+        line["bnb_c4"] = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample = cpu_sample_graphs(graphs)
