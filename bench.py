@@ -134,15 +134,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the DP tile kernel from the committed ncu
-    summary (profiles/dp_tile_kernel.md, line 'dram_bytes_per_launch_n30')."""
+def ncu_bytes_per_subset():
+    """DRAM bytes per subset of the DP tile kernel, measured by ncu on an
+    n = 28 launch (profiles/dp_tile_kernel.md, line 'dram_bytes_per_subset')."""
     path = os.path.join(ROOT, "profiles", "dp_tile_kernel.md")
     try:
         text = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_launch_n30:\s*([0-9.eE+]+)", text)
+    m = re.search(r"dram_bytes_per_subset:\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
 
 
@@ -383,7 +383,9 @@ def run_gpu(args, graphs):
     by_n_out = {str(n): {"dp_ms": statistics.median(x["dp_ms"] for x in v),
                          "alg_GBps": statistics.median(x["alg_bytes"] / (x["dp_ms"] / 1e3) / 1e9 for x in v)}
                 for n, v in sorted(by_n.items())}
-    traffic = ncu_traffic()
+    # ncu's DRAM bytes per subset (n = 28 capture) scaled to each launch's 2^n
+    bps = ncu_bytes_per_subset()
+    traffic = (bps * statistics.mean(2.0 ** g.n for g in graphs)) if bps else None
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
@@ -398,7 +400,10 @@ def run_gpu(args, graphs):
         "treedepths": tds,
         "roofline": {"bound": "hbm", "kernel": "dp_tile_kernel", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "alg_bytes_per_launch_mean": alg / launches,
+                     "traffic": traffic,
+                     "traffic_note": "ncu DRAM read+write bytes of an n=28 launch per subset, scaled by 2^n "
+                                     "and averaged over the workload's launches",
+                     "alg_bytes_per_launch_mean": alg / launches,
                      "launch_ms_mean": kms / launches, "by_n": by_n_out},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
