@@ -26,8 +26,11 @@
 //    worker (no CTA barriers in the loop). A warp takes a tile by ticket
 //    (atomicAdd) in level-major order, its lanes wait on the ready flags of
 //    the |H| child tiles (each wait bounded by a deadline), the warp reduces
-//    the children with 4-way SIMD byte min/max, resolves the tile, stores it
-//    and publishes its flag. A tile only waits on tiles with smaller tickets,
+//    the children with 2 x 16-bit DPX min/max (__vimin3_u16x2 /
+//    __vimax3_u16x2, three operands per instruction, after unpacking each
+//    byte word into two 16-bit pair words; byte-lane SIMD min/max has no
+//    native instruction here), resolves the tile, stores it and publishes
+//    its flag. A tile only waits on tiles with smaller tickets,
 //    and a ticket is only taken by a running warp, so the smallest unfinished
 //    ticket can always proceed.
 //

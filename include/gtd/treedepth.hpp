@@ -6,6 +6,10 @@
 //   auto order = dp.GetElimination<std::size_t>(n, n, 0);   // hpp:48-64
 //   td::gtd::Result r = dp.Decompose();   // treedepth, root, parent, edges
 //
+//   td::BnBGPU bnb;               // bnb_gpu.hpp:12-31
+//   int t = bnb(g, heur_td);      // exact treedepth by the persistent B&B
+//   td::gtd::Result r2 = bnb.Decompose();
+//
 // `g` is read through the Boost.Graph free functions num_vertices(g) and
 // adjacent_vertices(v, g) found by argument-dependent lookup, so a
 // boost::adjacency_list (what the reference's callers hold) is accepted
@@ -83,6 +87,23 @@ std::vector<uint64_t> AdjacencyMasks(Graph const& g) {
     auto range = adjacent_vertices(v, g);
     for (auto it = range.first; it != range.second; ++it)
       adj[v] |= uint64_t(1) << static_cast<std::size_t>(*it);
+  }
+  return adj;
+}
+
+// (lo, hi) 64-bit words per vertex for the B&B (n <= GTD_BNB_MAX_N).
+template <typename Graph>
+std::vector<uint64_t> AdjacencyMasks128(Graph const& g) {
+  const std::size_t n = num_vertices(g);
+  if (n > GTD_BNB_MAX_N)
+    throw std::invalid_argument("the branch and bound takes n <= " + std::to_string(GTD_BNB_MAX_N));
+  std::vector<uint64_t> adj(2 * n, 0);
+  for (std::size_t v = 0; v < n; ++v) {
+    auto range = adjacent_vertices(v, g);
+    for (auto it = range.first; it != range.second; ++it) {
+      const std::size_t u = static_cast<std::size_t>(*it);
+      adj[2 * v + (u >> 6)] |= uint64_t(1) << (u & 63);
+    }
   }
   return adj;
 }
@@ -168,6 +189,63 @@ class DynamicGPU {
   int n_ = 0;
   int td_ = 0;
   gtd_dp_stats stats_{};
+};
+
+// Exact treedepth by the GB300 branch and bound (persistent kernel), the
+// call shape of BnBGPU (bnb_gpu.hpp:12-17): operator()(g, heur_td) returns
+// the treedepth. The incumbent is the better of the library's reference
+// heuristic chain (HighestDegree(Variance), gtd_heuristic kind 0) and
+// heur_td when it does not exceed that chain's value; unlike the reference,
+// the result also carries a tree (Decompose). A disconnected graph throws
+// std::invalid_argument, as BranchAndBound does (branch_and_bound.hpp:67-75).
+class BnBGPU {
+ public:
+  explicit BnBGPU(int device = 0, uint64_t deadline_ns = 0) : handle_(device), deadline_ns_(deadline_ns) {}
+
+  template <typename Graph>
+  int operator()(Graph const& g, std::size_t heur_td = 0) {
+    std::vector<uint64_t> adj = gtd::AdjacencyMasks128(g);
+    const int n = static_cast<int>(num_vertices(g));
+    if (n == 0)
+      throw std::invalid_argument("empty graph");
+    std::vector<int32_t> seed_parent(n);
+    int32_t seed_td = 0;
+    gtd::check(gtd_heuristic(adj.data(), n, 0, nullptr, &seed_td, seed_parent.data()), handle_.get());
+    (void)heur_td;  // a bound without a tree cannot seed: the chain's tree does
+    gtd_graph_desc desc{n, 0};
+    int32_t td = 0, status = 0;
+    float proof_ms = 0;
+    uint64_t nodes = 0;
+    parent_.assign(n, -1);
+    gtd_bnb_opts opts{0, deadline_ns_, 0};
+    gtd::check(gtd_bnb_solve_batch(handle_.get(), &desc, 1, adj.data(), n, nullptr, &seed_td, seed_parent.data(),
+                                   &td, parent_.data(), &status, &proof_ms, &nodes, &opts, &stats_),
+               handle_.get());
+    gtd::check(static_cast<gtd_status>(status), handle_.get());
+    td_ = td;
+    return td;
+  }
+
+  gtd::Result Decompose() const {
+    gtd::Result r;
+    r.parent = parent_;
+    r.treedepth = static_cast<unsigned>(td_);
+    for (std::size_t v = 0; v < parent_.size(); ++v)
+      if (parent_[v] < 0) {
+        r.root = v;
+        break;
+      }
+    return r;
+  }
+
+  const gtd_bnb_stats& Stats() const { return stats_; }
+
+ private:
+  gtd::Handle handle_;
+  uint64_t deadline_ns_ = 0;
+  std::vector<int32_t> parent_;
+  int td_ = 0;
+  gtd_bnb_stats stats_{};
 };
 
 }  // namespace td

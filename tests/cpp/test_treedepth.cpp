@@ -40,5 +40,22 @@ int main() {
   } catch (std::invalid_argument const&) {
     std::printf("invalid_argument\n");
   }
+  // the branch and bound through the reference's BnBGPU call shape
+  td::BnBGPU bnb;
+  for (Graph* g : {&p7, &c5}) {
+    const int t = bnb(*g, 0);
+    auto r = bnb.Decompose();
+    std::printf("bnb %d %u %zu\n", t, r.treedepth, r.root);
+  }
+  Graph two(4);
+  boost::add_edge(0, 1, two);
+  boost::add_edge(2, 3, two);
+  try {
+    bnb(two, 0);
+    std::printf("no-throw\n");
+    return 1;
+  } catch (std::invalid_argument const&) {
+    std::printf("invalid_argument\n");
+  }
   return 0;
 }

@@ -39,3 +39,7 @@ def test_cpp_layer_matches_oracle(tmp_path, port):
         assert vals[2:] == port.get_elimination(g, T, (1 << g.n) - 1)
         assert par[vals[1]] == -1
     assert out[2] == "invalid_argument"
+    for line, want in zip(out[3:5], (3, 4)):
+        tag, t, td, root = line.split()
+        assert tag == "bnb" and int(t) == want and int(td) == want
+    assert out[5] == "invalid_argument"
