@@ -20,9 +20,11 @@
 //    all pass accepts C).
 //  * Bounds: the reference's edge bound in exact integer form
 //    (edge_lower_bound.hpp:13-20: smallest d with (d-1)(2n-d) >= 2e), a
-//    minor-min-width treewidth bound (td >= tw + 1), pendant vertices are
-//    never tried as roots of components with >= 3 vertices (their neighbour
-//    is at least as good), and a per-graph memo in HBM of a lower and an
+//    minor-min-width treewidth bound (td >= tw + 1), a longest-path bound
+//    (td >= ceil(log2(L + 1)) for a greedy path of L vertices, one walk per
+//    lane, tried when 2^k <= |C|), root domination (u is
+//    not tried as a root when N(u) lies in N[v] for a v of larger degree or
+//    equal degree and smaller id: v is at least as good), and a per-graph memo in HBM of a lower and an
 //    upper bound (with a root achieving it) per component, keyed by the
 //    component's vertex mask in 128-bit slots updated by atomic CAS and
 //    shared by every warp working on that graph.
@@ -318,6 +320,92 @@ struct Search {
     return __popcll(w->alo[v] & lo) + __popcll(w->ahi[v] & hi);
   }
 
+  // Longest-path bound: td(C) >= ceil(log2(L + 1)) for a path of L vertices
+  // in C (treedepth is monotone under subgraphs and td(P_L) = ceil(log2(L +
+  // 1))). Each lane grows one path greedily from its own start vertex,
+  // extending one end by the neighbour with the fewest unvisited neighbours
+  // (Warnsdorff's rule) until it is stuck, then the other end, and stops
+  // once the path has `need` vertices. The bound is the longest over lanes.
+  __device__ int path_lb(uint64_t Clo, uint64_t Chi, int need) const {
+    int start = -1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int u = lane + 32 * k;
+      if (start < 0 && u < n && has(Clo, Chi, u))
+        start = u;
+    }
+    uint32_t len = 0;
+    if (start >= 0) {
+      uint64_t plo = 0, phi = 0;
+      bit_set(plo, phi, start);
+      int e0 = start, e1 = start, side = 0, stuck = 0;
+      len = 1;
+      while (static_cast<int>(len) < need && stuck < 2) {
+        const int e = side ? e1 : e0;
+        uint64_t xlo = w->alo[e] & Clo & ~plo, xhi = w->ahi[e] & Chi & ~phi;
+        if (!(xlo | xhi)) {
+          ++stuck;
+          side ^= 1;
+          continue;
+        }
+        int best = -1, bd = 1 << 30;
+        while (xlo | xhi) {
+          const int x = first128(xlo, xhi);
+          bit_clear(xlo, xhi, x);
+          const int d = __popcll(w->alo[x] & Clo & ~plo) + __popcll(w->ahi[x] & Chi & ~phi);
+          if (d < bd) {
+            bd = d;
+            best = x;
+          }
+        }
+        bit_set(plo, phi, best);
+        if (side)
+          e1 = best;
+        else
+          e0 = best;
+        ++len;
+      }
+    }
+    len = __reduce_max_sync(0xffffffffu, len);
+    return 32 - __clz(static_cast<int>(len));
+  }
+
+  // Root domination (per lane, no warp collectives). If N_C(u) is contained
+  // in N_C[v] for some v != u in C, swapping u and v in any elimination tree
+  // of C rooted at u gives a valid tree of the same height rooted at v (v's
+  // edges reach everything from the root; each neighbour of u other than v
+  // is a neighbour of v, so it stays comparable with v's old position). So u
+  // need not be tried as a root. Such v have deg_C(v) >= deg_C(u); skipping
+  // u only for a v with a larger (degree, -id) keeps the chain of skips
+  // acyclic, so a non-skipped root at least as good always remains. The
+  // dominators of u are the intersection of N_C[w] over w in N_C(u).
+  __device__ bool dominated(int u, uint64_t Clo, uint64_t Chi) const {
+    uint64_t nlo = w->alo[u] & Clo, nhi = w->ahi[u] & Chi;
+    const int du = __popcll(nlo) + __popcll(nhi);
+    if (du == 0)
+      return false;
+    uint64_t ilo = Clo, ihi = Chi;
+    for (uint64_t m = nlo; m && (ilo | ihi); m &= m - 1) {
+      const int x = __ffsll(static_cast<long long>(m)) - 1;
+      ilo &= w->alo[x] | (1ull << x);
+      ihi &= w->ahi[x];
+    }
+    for (uint64_t m = nhi; m && (ilo | ihi); m &= m - 1) {
+      const int x = 64 + __ffsll(static_cast<long long>(m)) - 1;
+      ilo &= w->alo[x];
+      ihi &= w->ahi[x] | (1ull << (x - 64));
+    }
+    bit_clear(ilo, ihi, u);
+    while (ilo | ihi) {
+      const int v = first128(ilo, ihi);
+      bit_clear(ilo, ihi, v);
+      const int dv = deg_in(v, Clo, Chi);
+      if (dv > du || (dv == du && v < u))
+        return true;
+    }
+    return false;
+  }
+
   // Minor-min-width: repeatedly contract a minimum-degree vertex into its
   // minimum-degree neighbour; the largest minimum degree seen is a treewidth
   // lower bound, so td(C) >= it + 1.
@@ -421,14 +509,15 @@ struct Search {
   }
 
   // Next candidate of frame f: smallest rank >= f.nxt whose vertex is in C
-  // and is not a pendant vertex of a component with >= 3 vertices.
+  // and is not dominated as a root (a pendant vertex of a component with
+  // >= 3 vertices is dominated by its neighbour).
   __device__ int next_candidate(Frame& f, int csize) {
     for (int base = f.nxt; base < n; base += 32) {
       const int r = base + lane;
       bool ok = false;
       if (r < n) {
         const int v = w->order[r];
-        ok = has(f.lo, f.hi, v) && (csize < 3 || deg_in(v, f.lo, f.hi) != 1);
+        ok = has(f.lo, f.hi, v) && (csize < 3 || !dominated(v, f.lo, f.hi));
       }
       const uint32_t b = __ballot_sync(0xffffffffu, ok);
       if (b) {
@@ -524,6 +613,15 @@ struct Search {
                 lb = max(lb, mmd_lb(f.lo, f.hi));
                 if (lane == 0)
                   memo_put(memo, memo_mask, f.lo, f.hi, lb, kUnknownUb, 0);
+              }
+              // a path of 2^fk vertices would refute td <= fk
+              if (lb <= fk && fk < 7 && (1 << fk) <= csize) {
+                const int pl = path_lb(f.lo, f.hi, 1 << fk);
+                if (pl > fk) {
+                  lb = pl;
+                  if (lane == 0)
+                    memo_put(memo, memo_mask, f.lo, f.hi, lb, kUnknownUb, 0);
+                }
               }
               if (lb > fk)
                 verdict = 0;
@@ -767,8 +865,8 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
       s.stop.deadline = __shfl_sync(0xffffffffu, b, 0) + p.deadline_ns;
     }
     bool ok = false;
-    const bool pendant = G.n >= 3 && s.deg_in(v, fl, fh) == 1;  // dominated by its neighbour
-    if (!pendant)
+    const bool skip = G.n >= 3 && s.dominated(v, fl, fh);  // another root is at least as good
+    if (!skip)
       ok = s.decide(fl, fh, k, v, nullptr);
     // A success is published only with its tree: the first success of a
     // level claims the level's parent buffer and builds the tree while the
