@@ -65,8 +65,9 @@ def parse_args():
     ap.add_argument("--bnb-cap-s", type=float, default=10.0, help="B&B per-graph cap on time to proof")
     ap.add_argument("--bnb-memo-log2", type=int, default=0,
                     help="B&B memo slots per graph as a power of two (0 = sized from free HBM)")
-    ap.add_argument("--label-graphs", type=int, default=1500,
-                    help="graphs (n in [10, 24]) whose DP tables label the GNN training set")
+    ap.add_argument("--label-graphs", type=int, default=10000,
+                    help="graphs (n <= 24, config-2/3 families) whose DP tables label the GNN training set "
+                         "(each gives itself and 20 sampled subgraphs: ~200K labels at the default)")
     return ap.parse_args()
 
 
@@ -243,14 +244,15 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0):
     from gisbdw_gb300 import gnn
     from gisbdw_gb300 import graphs as G
     from gisbdw_gb300.validate import check_tree
+    base = gnn.training_graphs(n_label, seed=11)
     t0 = time.perf_counter()
-    samples = gnn.label_samples(h, G.config3_graphs(count=n_label, seed=11), per_graph=20, seed=1)
+    samples = gnn.label_set(h, base, per_graph=20, seed=1)
     t1 = time.perf_counter()
-    cut = len(samples) * 9 // 10
+    train_set, test_set = samples.split(0.9)
     net = gnn.GNN(h, seed=1)
-    losses = gnn.train(net, samples[:cut], epochs=8, batch_graphs=256, lr=3e-3)
+    losses = gnn.train(net, train_set, epochs=4, batch_graphs=256, lr=3e-3)
     t2 = time.perf_counter()
-    acc = gnn.root_accuracy(net, samples[cut:])
+    acc = gnn.root_accuracy(net, test_set)
     graphs = G.config4_graphs(count=n_graphs)
     cap_ns = int(cap_s * 1e9)
     h.bnb_solve_batch(graphs[:4], deadline_ns=10**8, memo_log2=memo_log2)  # warm-up (allocation, module load)

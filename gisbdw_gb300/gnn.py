@@ -51,6 +51,11 @@ def _bind(L):
     L.gtd_gnn_gradients.argtypes = [_vp, ctypes.POINTER(GnnBatch), ctypes.c_float, _vp, _vp]
     L.gtd_gnn_train_step.argtypes = [_vp, ctypes.POINTER(GnnBatch), ctypes.c_float, ctypes.c_float, _vp]
     L.gtd_dp_labels.argtypes = [_vp, _vp, ctypes.c_int, _vp, _vp]
+    L.gtd_gnn_features.argtypes = [_vp, ctypes.c_int, _vp]
+    L.gtd_gnn_pack_sizes.argtypes = [_vp, _vp, ctypes.c_int, _vp, _vp]
+    L.gtd_gnn_pack.argtypes = [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp]
+    L.gtd_gnn_make_labels.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                      ctypes.c_int, _vp, _vp, _vp, _vp, _vp]
     L._gnn_bound = True
     return L
 
@@ -130,24 +135,51 @@ class Batch:
                         _p(self.nbr_start), _p(self.nbr), _p(self.root_label), _p(self.node_mask), _p(self.td_label))
 
 
-def make_batch(graphs: Sequence[Graph], feats: Optional[Sequence[np.ndarray]] = None,
-               roots: Optional[Sequence[np.ndarray]] = None, tds: Optional[Sequence[int]] = None) -> Batch:
-    xs, starts, nstart, nbr = [], [0], [0], []
-    base = 0
-    for i, g in enumerate(graphs):
-        xs.append(feats[i] if feats is not None else features(g))
-        adj = g.adjacency_masks()
-        for v in range(g.n):
-            us = [base + u for u in range(g.n) if adj[v] >> u & 1]
-            nbr.extend(us)
-            nstart.append(nstart[-1] + len(us))
-        base += g.n
-        starts.append(base)
-    b = Batch(np.ascontiguousarray(np.concatenate(xs).astype(np.float32)), np.array(starts, dtype=np.int32),
-              np.array(nstart, dtype=np.int32), np.array(nbr if nbr else [0], dtype=np.int32))
+def native_features(g: Graph) -> np.ndarray:
+    """The library's features (gtd_gnn_features), the ones training and
+    inference use; `features` above is their Python statement."""
+    L = _bind(_lib.load())
+    adj = g.adj128()
+    x = np.zeros((g.n, IN_FEATURES), dtype=np.float32)
+    st = L.gtd_gnn_features(_p(adj), g.n, _p(x))
+    if st != 0:
+        raise _lib._error(st, "gtd_gnn_features failed")
+    return x
+
+
+def _descs(ns: np.ndarray, offs: np.ndarray) -> np.ndarray:
+    """gtd_graph_desc array ({int32 n, int32 offset} per graph)."""
+    return np.ascontiguousarray(np.stack([np.asarray(ns), np.asarray(offs)], axis=1).astype(np.int32))
+
+
+def pack(adj2: np.ndarray, ns: np.ndarray, offs: np.ndarray) -> Batch:
+    """Features and CSR neighbour lists (gtd_gnn_pack) of the graphs whose
+    (lo, hi) adjacency pairs start at adj2[2 * offs[i]]."""
+    L = _bind(_lib.load())
+    count = len(ns)
+    descs = _descs(ns, offs)
+    nodes, nbrs = ctypes.c_int64(), ctypes.c_int64()
+    dp = _p(descs)
+    st = L.gtd_gnn_pack_sizes(_p(adj2), dp, count, ctypes.byref(nodes), ctypes.byref(nbrs))
+    if st != 0:
+        raise _lib._error(st, "gtd_gnn_pack_sizes failed")
+    b = Batch(np.zeros((nodes.value, IN_FEATURES), dtype=np.float32), np.zeros(count + 1, dtype=np.int32),
+              np.zeros(nodes.value + 1, dtype=np.int32), np.zeros(max(1, nbrs.value), dtype=np.int32))
+    st = L.gtd_gnn_pack(_p(adj2), dp, count, _p(b.x), _p(b.graph_start), _p(b.nbr_start), _p(b.nbr))
+    if st != 0:
+        raise _lib._error(st, "gtd_gnn_pack failed")
+    return b
+
+
+def make_batch(graphs: Sequence[Graph], roots: Optional[Sequence[np.ndarray]] = None,
+               tds: Optional[Sequence[int]] = None) -> Batch:
+    ns = np.array([g.n for g in graphs], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+    adj2 = np.concatenate([g.adj128() for g in graphs]).astype(np.uint64)
+    b = pack(adj2, ns, offs)
     if roots is not None:
         b.root_label = np.concatenate(roots).astype(np.float32)
-        b.node_mask = np.ones(base, dtype=np.float32)
+        b.node_mask = np.ones(int(ns.sum()), dtype=np.float32)
         b.td_label = np.array(tds, dtype=np.float32)
     return b
 
@@ -303,89 +335,134 @@ def reference_loss(params: np.ndarray, b: Batch, shape=(IN_FEATURES, HIDDEN, LAY
 # Labels from the exact DP, training, and use in the branch and bound.
 # ---------------------------------------------------------------------------
 
-def _induced(g: Graph, mask: int) -> Tuple[Graph, List[int]]:
-    verts = [v for v in range(g.n) if mask >> v & 1]
-    idx = {v: i for i, v in enumerate(verts)}
-    edges = [(idx[u], idx[v]) for u, v in g.edges if u in idx and v in idx]
-    return Graph(len(verts), edges), verts
+@dataclass
+class LabelSet:
+    """Samples (connected induced subgraph, optimal-root mask, td) from the
+    exact DP: graph i has ns[i] vertices whose (lo, hi) adjacency pairs start
+    at adj2[2 * offs[i]]."""
+    adj2: np.ndarray
+    ns: np.ndarray
+    offs: np.ndarray
+    roots: np.ndarray
+    td: np.ndarray
+
+    def __len__(self) -> int:
+        return len(self.ns)
+
+    def take(self, idx) -> "LabelSet":
+        return LabelSet(self.adj2, self.ns[idx], self.offs[idx], self.roots[idx], self.td[idx])
+
+    def split(self, frac: float) -> Tuple["LabelSet", "LabelSet"]:
+        cut = int(len(self) * frac)
+        return self.take(slice(0, cut)), self.take(slice(cut, len(self)))
+
+    def packed(self) -> Batch:
+        """Features and CSR lists of every sample, packed once (gtd_gnn_pack)."""
+        if getattr(self, "_packed", None) is None:
+            self._packed = pack(self.adj2, self.ns, self.offs)
+        return self._packed
+
+    def batch(self, idx=None) -> Batch:
+        """The samples idx as one batch, gathered from the packed set."""
+        P = self.packed()
+        idx = np.arange(len(self)) if idx is None else np.asarray(idx)
+        lens = self.ns[idx].astype(np.int64)
+        starts = P.graph_start[idx].astype(np.int64)
+        gs = np.zeros(len(idx) + 1, dtype=np.int64)
+        np.cumsum(lens, out=gs[1:])
+        total = int(gs[-1])
+        shift = np.repeat(gs[:-1] - starts, lens)             # old node index -> batch index
+        node = np.arange(total, dtype=np.int64) - shift       # old index of every batch node
+        deg = (P.nbr_start[node + 1] - P.nbr_start[node]).astype(np.int64)
+        ns_ = np.zeros(total + 1, dtype=np.int64)
+        np.cumsum(deg, out=ns_[1:])
+        edge = np.arange(int(ns_[-1]), dtype=np.int64) - np.repeat(ns_[:-1] - P.nbr_start[node], deg)
+        nbr = P.nbr[edge] + np.repeat(shift, deg)
+        b = Batch(np.ascontiguousarray(P.x[node]), gs.astype(np.int32), ns_.astype(np.int32),
+                  np.ascontiguousarray(nbr.astype(np.int32)) if len(nbr) else np.zeros(1, dtype=np.int32))
+        local = (np.arange(total, dtype=np.int64) - np.repeat(gs[:-1], lens)).astype(np.uint64)
+        b.root_label = ((np.repeat(self.roots[idx], lens) >> local) & np.uint64(1)).astype(np.float32)
+        b.node_mask = np.ones(total, dtype=np.float32)
+        b.td_label = self.td[idx].astype(np.float32)
+        return b
+
+    def graph(self, i: int) -> Graph:
+        n, o = int(self.ns[i]), int(self.offs[i])
+        a = self.adj2[2 * o:2 * (o + n):2]
+        return Graph(n, [(u, v) for u in range(n) for v in range(u + 1, n) if int(a[u]) >> v & 1])
 
 
-def _random_connected_subset(g: Graph, adj: List[int], size: int, rng: np.random.Generator) -> int:
-    start = int(rng.integers(g.n))
-    S = 1 << start
-    frontier = adj[start]
-    while bin(S).count("1") < size and frontier & ~S:
-        cand = [u for u in range(g.n) if (frontier & ~S) >> u & 1]
-        u = cand[int(rng.integers(len(cand)))]
-        S |= 1 << u
-        frontier |= adj[u]
-    return S
-
-
-def label_samples(handle: _lib.Handle, graphs: Sequence[Graph], per_graph: int, seed: int = 0,
-                  min_size: int = 5):
-    """(subgraph, root-label vector, td) samples: for every graph (n <= 24),
-    the whole graph plus `per_graph` random connected induced subgraphs,
-    labelled from the exact DP table on the GPU."""
-    L = _bind(handle.L)
-    rng = np.random.default_rng(seed)
-    out = []
-    for g in graphs:
-        if g.n > 24:
-            raise ValueError("label graphs must have n <= 24")
-        handle.dp_solve(g.adj64(), g.n, want_order=False)
-        adj = g.adjacency_masks()
-        masks = {(1 << g.n) - 1}
-        for _ in range(per_graph):
-            size = int(rng.integers(min(min_size, g.n), g.n + 1))
-            masks.add(_random_connected_subset(g, adj, size, rng))
-        ms = np.array(sorted(masks), dtype=np.uint64)
-        td = np.zeros(len(ms), dtype=np.int32)
-        roots = np.zeros(len(ms), dtype=np.uint64)
-        handle._check(L.gtd_dp_labels(handle._h, _p(ms), len(ms), _p(td), _p(roots)))
-        for m, t, r in zip(ms.tolist(), td.tolist(), roots.tolist()):
-            sub, verts = _induced(g, m)
-            if sub.n < 2 or not sub.is_connected():
-                continue
-            y = np.array([(r >> v) & 1 for v in verts], dtype=np.float32)
-            out.append((sub, y, t))
+def training_graphs(count: int, seed: int = 11) -> List[Graph]:
+    """Label base graphs (n <= 24) of the config-2 and config-3 families:
+    every other one a config-3 graph (G(n, p), tree plus extra edges, deleted
+    grid; n in [10, 24]), the rest connected G(n, p) with n in [16, 24] and
+    p in {0.1, 0.2, 0.3} like the config-2 graphs."""
+    from . import graphs as G
+    half = count // 2
+    out = G.config3_graphs(count=count - half, seed=seed)
+    for i in range(half):
+        n = 16 + (i * 7 + seed) % 9
+        p = (0.1, 0.2, 0.3)[i % 3]
+        out.append(G.gnp_connected(n, p, 50000 + 97 * seed + i))
     return out
 
 
-def train(net: GNN, samples, epochs: int = 4, batch_graphs: int = 256, lr: float = 3e-3, seed: int = 0,
+def label_set(handle: _lib.Handle, graphs: Sequence[Graph], per_graph: int, seed: int = 0,
+              min_size: int = 5) -> LabelSet:
+    """Every graph (n <= 24) and `per_graph` random connected induced
+    subgraphs of it, labelled from the exact DP on the GPU
+    (gtd_gnn_make_labels)."""
+    L = _bind(handle.L)
+    ns = np.array([g.n for g in graphs], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+    adj2 = np.concatenate([g.adj128() for g in graphs]).astype(np.uint64)
+    descs = _descs(ns, offs)
+    cap = len(graphs) * (per_graph + 1)
+    sub_adj = np.zeros(2 * 24 * cap, dtype=np.uint64)
+    sub_desc = np.zeros((cap, 2), dtype=np.int32)
+    roots = np.zeros(cap, dtype=np.uint64)
+    td = np.zeros(cap, dtype=np.int32)
+    num = ctypes.c_int()
+    handle._check(L.gtd_gnn_make_labels(handle._h, _p(adj2), _p(descs), len(graphs), per_graph, min_size, seed, cap,
+                                        _p(sub_adj), _p(sub_desc), _p(roots), _p(td), ctypes.byref(num)))
+    k = num.value
+    sns = sub_desc[:k, 0].astype(np.int64)
+    soffs = sub_desc[:k, 1].astype(np.int64)
+    used = int((soffs[-1] + sns[-1]) if k else 0)
+    return LabelSet(sub_adj[:2 * used].copy(), sns, soffs, roots[:k].copy(), td[:k].copy())
+
+
+def train(net: GNN, data: LabelSet, epochs: int = 4, batch_graphs: int = 256, lr: float = 3e-3, seed: int = 0,
           td_weight: float = 0.05) -> List[float]:
     rng = np.random.default_rng(seed)
-    feats = [features(s[0]) for s in samples]
     losses = []
     for _ in range(epochs):
-        order = rng.permutation(len(samples))
+        order = rng.permutation(len(data))
         for i in range(0, len(order), batch_graphs):
-            idx = order[i:i + batch_graphs]
-            b = make_batch([samples[j][0] for j in idx], [feats[j] for j in idx],
-                           [samples[j][1] for j in idx], [samples[j][2] for j in idx])
-            losses.append(net.train_step(b, lr=lr, td_weight=td_weight))
+            losses.append(net.train_step(data.batch(order[i:i + batch_graphs]), lr=lr, td_weight=td_weight))
     return losses
 
 
-def root_accuracy(net: GNN, samples) -> dict:
+def root_accuracy(net: GNN, data: LabelSet) -> dict:
     """Fraction of samples whose top-scored vertex is an optimal root, the
     same for a max-degree pick and a uniform pick, and the td estimate's mean
     absolute error."""
     hits = deg_hits = rand = 0.0
-    td_err = []
-    for i in range(0, len(samples), 512):
-        chunk = samples[i:i + 512]
-        b = make_batch([s[0] for s in chunk])
+    err = []
+    for i in range(0, len(data), 4096):
+        idx = np.arange(i, min(len(data), i + 4096))
+        b = data.batch(idx)
         logits, td = net.forward(b)
-        for k, (g, y, t) in enumerate(chunk):
+        y = b.root_label
+        for k in range(len(idx)):
             s, e = b.graph_start[k], b.graph_start[k + 1]
-            hits += y[int(np.argmax(logits[s:e]))]
-            deg_hits += y[int(np.argmax(g.degrees()))]
-            rand += y.mean()
-            td_err.append(abs(float(td[k]) - t))
-    n = max(1, len(samples))
+            hits += y[s + int(np.argmax(logits[s:e]))]
+            deg_hits += y[s + int(np.argmax(b.x[s:e, 0]))]
+            rand += float(y[s:e].mean())
+        err.append(np.abs(td - b.td_label))
+    n = max(1, len(data))
     return {"top1_root": float(hits) / n, "max_degree_root": float(deg_hits) / n, "uniform_root": float(rand) / n,
-            "td_mae": float(np.mean(td_err)) if td_err else None, "samples": len(samples)}
+            "td_mae": float(np.concatenate(err).mean()) if err else None, "samples": len(data)}
 
 
 def orders_and_seeds(net: GNN, graphs: Sequence[Graph]):

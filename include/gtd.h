@@ -272,6 +272,34 @@ gtd_status gtd_gnn_gradients(gtd_gnn g, const gtd_gnn_batch* b,
 gtd_status gtd_gnn_train_step(gtd_gnn g, const gtd_gnn_batch* b, float lr,
                               float td_weight, float* loss_out);
 
+/* Host data pipeline of the GNN (n <= 128 per graph, adjacency as (lo, hi)
+ * pairs per vertex like gtd_bnb_solve_batch). Features per vertex (8):
+ * degree / 4, core number / 4, eccentricity / 8, mean neighbour degree / 4,
+ * pendant flag, 1 / (1 + degree), n / 64, 1. */
+gtd_status gtd_gnn_features(const uint64_t* adj2, int n, float* x_out);
+/* Sizes of a packed batch: total vertices and total neighbour entries. */
+gtd_status gtd_gnn_pack_sizes(const uint64_t* adj2_pool,
+                              const gtd_graph_desc* descs, int count,
+                              int64_t* nodes_out, int64_t* nbrs_out);
+/* Features and CSR neighbour lists of graphs (the x / graph_start /
+ * nbr_start / nbr arrays of a gtd_gnn_batch). */
+gtd_status gtd_gnn_pack(const uint64_t* adj2_pool, const gtd_graph_desc* descs,
+                        int count, float* x_out, int32_t* graph_start_out,
+                        int32_t* nbr_start_out, int32_t* nbr_out);
+/* Training labels from the exact DP: every base graph (2 <= n <= 24) is
+ * solved on the GPU, then it and per_graph random connected induced
+ * subgraphs (sizes uniform in [min_size, n], grown from a random vertex) are
+ * labelled with td and the optimal-root mask (gtd_dp_labels). Up to
+ * `capacity` samples are written relabelled 0..k-1 in vertex order:
+ * sub_adj2_out (capacity * 48 words), sub_desc_out, root_out, td_out;
+ * *num_out = samples written. Uses (and overwrites) the handle's DP table. */
+gtd_status gtd_gnn_make_labels(gtd_handle h, const uint64_t* adj2_pool,
+                               const gtd_graph_desc* descs, int count,
+                               int per_graph, int min_size, uint64_t seed,
+                               int capacity, uint64_t* sub_adj2_out,
+                               gtd_graph_desc* sub_desc_out, uint64_t* root_out,
+                               int32_t* td_out, int* num_out);
+
 /* Largest n gtd_dp_solve_noalloc accepts (its fixed scratch holds a 2^n-byte
  * table: 16 MiB at n = 24). */
 #define GTD_DP_NOALLOC_MAX_N 24

