@@ -53,7 +53,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gtd", choices=["gtd", "reference"])
-    ap.add_argument("--workload", default="dp-c2", choices=["dp-c2"])
+    ap.add_argument("--workload", default="dp-c2", choices=["dp-c2", "bnb-c5"],
+                    help="dp-c2: the default line; bnb-c5: the config-5 B&B stream")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-n", type=int, default=0,
                     help="restrict the workload to its graphs with this n (profiling)")
@@ -61,14 +62,25 @@ def parse_args():
                     help="DP tile bits (0 = the library's default)")
     ap.add_argument("--no-c3", action="store_true", help="skip the batched DP measurement")
     ap.add_argument("--no-bnb", action="store_true", help="skip the plain vs learned B&B measurement")
-    ap.add_argument("--bnb-graphs", type=int, default=256, help="B&B graphs (config 4 family)")
-    ap.add_argument("--bnb-cap-s", type=float, default=10.0, help="B&B per-graph cap on time to proof")
+    ap.add_argument("--bnb-graphs", type=int, default=None,
+                    help="B&B graphs (default 256 of config 4; 1024 of config 5 with --workload bnb-c5)")
+    ap.add_argument("--bnb-cap-s", type=float, default=None,
+                    help="B&B per-graph cap on time to proof (default 10 s; 60 s with --workload bnb-c5)")
+    ap.add_argument("--cpu-bnb-sample", type=int, default=32, help="config-4 graphs in the CPU B&B baseline")
+    ap.add_argument("--cpu-bnb-nodes", type=int, default=20_000_000,
+                    help="search-node cap per graph of the CPU B&B baseline")
     ap.add_argument("--bnb-memo-log2", type=int, default=0,
                     help="B&B memo slots per graph as a power of two (0 = sized from free HBM)")
     ap.add_argument("--label-graphs", type=int, default=10000,
                     help="graphs (n <= 24, config-2/3 families) whose DP tables label the GNN training set "
                          "(each gives itself and 20 sampled subgraphs: ~200K labels at the default)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    c5 = args.workload == "bnb-c5"
+    if args.bnb_graphs is None:
+        args.bnb_graphs = 1024 if c5 else 256
+    if args.bnb_cap_s is None:
+        args.bnb_cap_s = 60.0 if c5 else 10.0
+    return args
 
 
 def dist_env():
@@ -180,6 +192,26 @@ def time_cpu_dp(graphs, steps, threads):
     return times, tds
 
 
+def time_cpu_bnb(graphs, node_limit, threads):
+    """The oracle's restatement of the reference BranchAndBound (EdgeLowerBound,
+    HighestDegree(Variance) incumbent) on `threads` host threads, one graph per
+    thread at a time, each capped at node_limit search nodes."""
+    from concurrent.futures import ThreadPoolExecutor
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    port = oracle.Port()
+
+    def one(g):
+        t0 = time.perf_counter()
+        st, td, _, nodes = port.bnb(g, node_limit=node_limit)
+        return st, td, nodes, time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:  # ctypes calls release the GIL
+        res = list(ex.map(one, graphs))
+    return res, time.perf_counter() - t0
+
+
 def run_reference(args, graphs):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -237,9 +269,10 @@ def measure_dp_c3(h, steps, warmup):
             "trees_invalid": bad}
 
 
-def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0):
-    """Plain vs learned-guided B&B on the config 4 family (identical graphs),
-    the GNN trained here on DP labels."""
+def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_nodes=0, family="c4"):
+    """Plain vs learned-guided B&B on the config 4 family (or the config 5
+    stream; identical graphs in both arms), the GNN trained here on DP
+    labels."""
     import numpy as np
     from gisbdw_gb300 import gnn
     from gisbdw_gb300 import graphs as G
@@ -253,7 +286,7 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0):
     losses = gnn.train(net, train_set, epochs=4, batch_graphs=256, lr=3e-3)
     t2 = time.perf_counter()
     acc = gnn.root_accuracy(net, test_set)
-    graphs = G.config4_graphs(count=n_graphs)
+    graphs = G.config4_graphs(count=n_graphs) if family == "c4" else G.config5_graphs(count=n_graphs)
     cap_ns = int(cap_s * 1e9)
     h.bnb_solve_batch(graphs[:4], deadline_ns=10**8, memo_log2=memo_log2)  # warm-up (allocation, module load)
     plain = h.bnb_solve_batch(graphs, deadline_ns=cap_ns, memo_log2=memo_log2)
@@ -266,7 +299,7 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0):
         ok = res["status"] == 0
         pm = res["proof_ms"]
         fam = {}
-        for f in ("rgg", "reg3", "grid"):
+        for f in ("rgg", "reg3", "grid", "tree"):
             sel = np.array([g.name.startswith(f) for g in graphs])
             fam[f] = f"{int((ok & sel).sum())}/{int(sel.sum())}"
         return {"solved": int(ok.sum()), "solves_per_s": float(ok.sum() / (res["stats"]["ms"] / 1e3)),
@@ -287,6 +320,22 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0):
     if both.any():
         pp, lp = np.median(plain["proof_ms"][both]), np.median(learned["proof_ms"][both])
         out["p50_proof_ms_both"] = {"plain": float(pp), "learned": float(lp), "plain_over_learned": float(pp / lp)}
+    if cpu_sample:
+        threads = os.cpu_count() or 1
+        sample = graphs[:cpu_sample]
+        res, wall = time_cpu_bnb(sample, cpu_nodes, threads)
+        solved = [r[0] == 0 for r in res]
+        gpu_td = {i: int(learned["td"][i]) for i in range(len(sample)) if learned["status"][i] == 0}
+        out["cpu_baseline"] = {
+            "value": sum(solved) / wall, "unit": "solves/s", "cores": threads, "kind": "port",
+            "solved": int(sum(solved)), "of": len(sample), "wall_s": wall, "node_limit": cpu_nodes,
+            "nodes_per_s": sum(r[2] for r in res) / sum(r[3] for r in res),
+            "gpu_learned_solved_in_sample": int((learned["status"][:len(sample)] == 0).sum()),
+            "gpu_plain_solved_in_sample": int((plain["status"][:len(sample)] == 0).sum()),
+            "td_agree": all(r[1] == gpu_td[i] for i, r in enumerate(res) if r[0] == 0 and i in gpu_td),
+            "sample": f"first {len(sample)} config-4 graphs; oracle restatement of BranchAndBound "
+                      f"(branch_and_bound.cpp:51-114, EdgeLowerBound, HighestDegree(Variance)), "
+                      f"{cpu_nodes} nodes per graph, {threads} host threads ({cpu_model()})"}
     return out
 
 
@@ -415,7 +464,8 @@ def run_gpu(args, graphs):
     if rank == 0 and not args.no_c3:
         line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup)
     if rank == 0 and not args.no_bnb:
-        line["bnb_c4"] = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2)
+        line["bnb_c4"] = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
+                                     0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample = cpu_sample_graphs(graphs)
@@ -433,9 +483,52 @@ def run_gpu(args, graphs):
         torch.distributed.destroy_process_group()
 
 
+def run_bnb_stream(args):
+    """--workload bnb-c5: the config-5 mixed stream (1024 graphs, n in
+    [20, 80], 60 s per-graph cap) solved in one persistent B&B launch per arm;
+    the headline is the learned arm's proven solves/s."""
+    import torch
+    from gisbdw_gb300 import Handle
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    h = Handle(local)
+    sampler = ClockSampler(local)
+    sampler.start()
+    r = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
+                    0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes, family="c5")
+    clocks = sampler.stop()
+    L = r["learned"]
+    line = {
+        "metric": METRIC, "value": L["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": L["batch_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int (bit masks)", "data": "synthetic",
+        "config": {"workload": f"bnb-c5 (config 5: {r['graphs']} graphs, n in [20, 80], random geometric / "
+                               f"3-regular / deleted grids / trees plus edges; {args.bnb_cap_s:g} s per-graph cap)",
+                   "l2": "search state in shared memory, memo in HBM"},
+        "p50_time_to_proof_ms": L["p50_proof_ms_capped"], "bnb": r, "roofline": None,
+        "roofline_note": "integer-issue-bound search (profiles/bnb_kernel.md); no byte or FLOP roofline applies",
+        "e2e": {"value": L["e2e_solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None},
+        "gpu_launches": 4, "clocks": clocks,
+    }
+    if "cpu_baseline" in r:
+        line["cpu_baseline"] = r["cpu_baseline"]
+    print(json.dumps(line), flush=True)
+    h.close()
+
+
 def main():
     args = parse_args()
     from gisbdw_gb300 import graphs as G
+    if args.workload == "bnb-c5":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the config-5 CPU B&B is reported inside the "
+                              "gtd line's cpu_baseline"}), flush=True)
+            return
+        run_bnb_stream(args)
+        return
     graphs = G.config2_graphs()
     if args.only_n:
         graphs = [g for g in graphs if g.n == args.only_n]
