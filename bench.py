@@ -291,9 +291,10 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     h.bnb_solve_batch(graphs[:4], deadline_ns=10**8, memo_log2=memo_log2)  # warm-up (allocation, module load)
     plain = h.bnb_solve_batch(graphs, deadline_ns=cap_ns, memo_log2=memo_log2)
     t3 = time.perf_counter()
-    orders, seeds = gnn.orders_and_seeds(net, graphs)
+    gd = gnn.guidance(net, graphs)
     t_inf = time.perf_counter() - t3
-    learned = h.bnb_solve_batch(graphs, orders=orders, seeds=seeds, deadline_ns=cap_ns, memo_log2=memo_log2)
+    learned = h.bnb_solve_batch(graphs, orders=gd["orders"], seeds=gd["seeds"], hints=gd["hints"],
+                                deadline_ns=cap_ns, memo_log2=memo_log2)
 
     def summary(res, extra_s=0.0):
         ok = res["status"] == 0
@@ -311,6 +312,9 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
                 "trees_valid": all(check_tree(g, int(t), par) for g, t, par in
                                    zip(graphs, res["td"], res["parents"]))}
     ps, ls = summary(plain), summary(learned, t_inf)
+    solved = learned["status"] == 0
+    ls["td_estimate_mae_on_proven"] = float(np.abs(gd["td_est"][solved] - learned["td"][solved]).mean()) \
+        if solved.any() else None
     both = (plain["status"] == 0) & (learned["status"] == 0)
     out = {"graphs": len(graphs), "cap_s": cap_s, "plain": ps, "learned": ls, "both_solved": int(both.sum()),
            "td_identical_on_both": bool(np.array_equal(plain["td"][both], learned["td"][both])),

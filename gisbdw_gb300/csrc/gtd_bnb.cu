@@ -28,9 +28,18 @@
 //    upper bound (with a root achieving it) per component, keyed by the
 //    component's vertex mask in 128-bit slots updated by atomic CAS and
 //    shared by every warp working on that graph.
-//  * Schedule: one persistent launch over a global atomic queue of items
+//  * Schedule: persistent launches over a global atomic queue of items
 //    (graph, level k, root candidate), issued for k descending from the
 //    incumbent minus one, candidates in priority order, graphs interleaved.
+//    Passes: an item may spend a node budget per launch; an item that spends
+//    it stops and is issued again in the next launch with twice its own
+//    budget (the memo keeps every subproblem it settled, so the rerun
+//    resumes cheaply). Only a window of W levels per graph runs at a time:
+//    k in (top - W, top], top = best - 1, or a caller's level hint clamped
+//    into [proven lower bound, best - 1] (the learned td estimate: it orders
+//    which decisions run first and never prunes; a wrong hint only moves the
+//    window). Easy graphs finish in the first passes instead of waiting
+//    behind the long items of hard graphs.
 //    A success at level k improves the graph's best (atomicMin) and
 //    cancels every remaining item at levels >= k; when every candidate at
 //    level k has failed, the graph's proven lower bound becomes k + 1 and
@@ -60,6 +69,12 @@ constexpr int kMemoProbes = 8;
 constexpr int kMmdMin = 10;              // minor-min-width bound for |C| >= this
 constexpr uint32_t kSeedRoot = 0xFFu;
 constexpr int kUnknownUb = 127;
+constexpr int kIoUnfinished = 3;         // d_io word: items that spent their budget this round
+constexpr uint64_t kFirstBudget = 1024;  // search nodes of an item's first run
+constexpr uint32_t kMaxDoublings = 30;   // an item's budget grows to at most 2^30 times the first
+constexpr uint32_t kItemDone = 0xFF;
+constexpr int kRoundWindow = 3;          // levels run at a time per graph
+constexpr int kMaxRounds = 4096;
 
 enum BnbStatus : int32_t { kBnbRunning = 0, kBnbTimeout = 2 };
 
@@ -70,7 +85,7 @@ struct BnbGraph {
   int32_t n;
   int32_t lb0;         // lower bound of the whole graph
   int32_t ub0;         // incumbent (seed) treedepth
-  int32_t pad;
+  int32_t hint;        // level to try first (0 = none: top-down from the incumbent)
 };
 
 struct BnbParams {
@@ -86,6 +101,10 @@ struct BnbParams {
   uint32_t* lbp = nullptr;         // per graph: proven lower bound
   uint32_t* fails = nullptr;       // per graph x level: failed candidates
   uint32_t* claim = nullptr;       // per graph x level: tree buffer taken
+  uint8_t* item_state = nullptr;   // per graph x level x rank: kItemDone, or the item's budget doublings so far
+  uint64_t budget = 0;             // an item's first budget in search nodes (0 = unlimited)
+  int window = 0;                  // levels run at a time below a graph's top level (0 = all)
+  uint32_t* unfinished = nullptr;  // items that used up their budget this round
   int8_t* lvl_parent = nullptr;    // per graph x level: tree (max_n entries, -1 root)
   int32_t* status = nullptr;       // per graph BnbStatus
   uint64_t* t_begin = nullptr;     // per graph: first item start (globaltimer ns)
@@ -257,6 +276,7 @@ struct StopCheck {
   const uint32_t* lbp = nullptr;   // stop when proven lb > item_k
   int item_k = 0;
   uint64_t deadline = 0;           // absolute ns, 0 = none
+  uint64_t budget = 0;             // nodes before the item yields, 0 = none
 };
 
 struct Search {
@@ -267,6 +287,7 @@ struct Search {
   StopCheck stop;
   unsigned long long nodes;
   bool timed_out, cancelled;
+  bool yielded = false;
 
   __device__ void component(uint64_t Slo, uint64_t Shi, int v, uint64_t& rlo, uint64_t& rhi) const {
     rlo = v < 64 ? (1ull << v) : 0ull;
@@ -536,7 +557,8 @@ struct Search {
     return -1;
   }
 
-  // Every 64 nodes: deadline, or the item became useless.
+  // Every 64 nodes: deadline, the item became useless, or its node budget
+  // for this round is spent.
   __device__ bool should_stop() {
     if (nodes & 63)
       return false;
@@ -544,6 +566,8 @@ struct Search {
     if (lane == 0) {
       if (stop.deadline && global_ns() > stop.deadline)
         flag = 1;
+      else if (stop.budget && nodes >= stop.budget)
+        flag = 3;
       else if ((stop.best && static_cast<int>(ld_acquire_u32(stop.best) >> 8) <= stop.item_k) ||
                (stop.lbp && static_cast<int>(ld_acquire_u32(stop.lbp)) > stop.item_k))
         flag = 2;
@@ -553,6 +577,8 @@ struct Search {
       timed_out = true;
     if (flag == 2)
       cancelled = true;
+    if (flag == 3)
+      yielded = true;
     return flag != 0;
   }
 
@@ -731,7 +757,7 @@ struct Search {
     }
     if (root_out)
       *root_out = ret_root;
-    return ret && !timed_out && !cancelled;
+    return ret && !timed_out && !cancelled && !yielded;
   }
 
   // Elimination tree of C (depth <= k) below the accepted root: every
@@ -836,17 +862,33 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
     const int k = G.ub0 - 1 - li;
     if (r >= G.n || k < G.lb0)
       continue;
+    const size_t item_idx = (size_t(g) * p.levels + li) * p.max_n + r;
+    const uint32_t istate = p.item_state[item_idx];
+    if (istate == kItemDone)
+      continue;  // finished in an earlier round
     int useful = 0;
     if (lane == 0) {
       const unsigned long long now = global_ns();
       atomicMin(p.t0, now);
       atomicCAS(reinterpret_cast<unsigned long long*>(p.t_begin + g), 0ull, now);
-      useful = static_cast<int>(ld_acquire_u32(p.best + g) >> 8) > k &&
-               static_cast<int>(ld_acquire_u32(p.lbp + g)) <= k && ld_relaxed_s32(p.status + g) != kBnbTimeout;
+      const int bk = static_cast<int>(ld_acquire_u32(p.best + g) >> 8);
+      const int lk = static_cast<int>(ld_acquire_u32(p.lbp + g));
+      useful = bk > k && lk <= k && ld_relaxed_s32(p.status + g) != kBnbTimeout;
+      // window: the top level is best - 1, or the hint clamped into [lbp, best - 1]
+      const int top = G.hint > 0 ? min(bk - 1, max(G.hint, lk)) : bk - 1;
+      if (useful && p.window && (k > top || k <= top - p.window))
+        useful = 2;  // outside the window: a later pass
     }
     useful = __shfl_sync(0xffffffffu, useful, 0);
-    if (!useful)
+    if (useful == 2)
       continue;
+    if (!useful) {
+      // best only falls, the proven bound only rises and a timeout is final:
+      // a useless item stays useless
+      if (lane == 0)
+        p.item_state[item_idx] = kItemDone;
+      continue;
+    }
     if (g != cur_g) {
       load_graph(w, p, G, lane);
       cur_g = g;
@@ -858,6 +900,7 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
     s.stop.best = p.best + g;
     s.stop.lbp = p.lbp + g;
     s.stop.item_k = k;
+    s.stop.budget = p.budget ? (p.budget << istate) : 0;
     if (p.deadline_ns) {
       uint64_t b = 0;
       if (lane == 0)
@@ -880,6 +923,7 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
       claimed = __shfl_sync(0xffffffffu, claimed, 0);
       if (claimed) {
         int8_t* tree = p.lvl_parent + (size_t(g) * p.levels + li) * p.max_n;
+        s.stop.budget = 0;  // the tree is mostly memo hits: no yield half way
         publish = s.build_tree(fl, fh, k, v, tree);
         if (!publish && !s.timed_out && !s.cancelled && lane == 0)
           raise_error(p.error, kDevNoRoot, g);
@@ -888,9 +932,15 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
     }
     if (lane == 0) {
       atomicAdd(p.nodes + g, s.nodes);
+      if (s.yielded && !s.timed_out && !s.cancelled) {
+        atomicAdd(p.unfinished, 1u);  // run again next pass with twice the budget
+        p.item_state[item_idx] = static_cast<uint8_t>(min(istate + 1, kMaxDoublings));
+      } else {
+        p.item_state[item_idx] = kItemDone;
+      }
       if (s.timed_out) {
         atomicExch(p.status + g, kBnbTimeout);
-      } else if (!s.cancelled) {
+      } else if (!s.cancelled && !s.yielded) {
         if (ok) {
           if (publish)
             atomicMin(p.best + g, (static_cast<uint32_t>(k) << 8) | static_cast<uint32_t>(v));
@@ -1126,6 +1176,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
       e += __builtin_popcountll(a[2 * v]) + __builtin_popcountll(a[2 * v + 1]);
     G.lb0 = std::max(edge_lb_host(d.n, e / 2), d.n >= 2 ? mmd_host(a, d.n) : 1);
     G.ub0 = seed_td[i];
+    G.hint = (opts && opts->level_hint) ? std::max(0, std::min(opts->level_hint[i], d.n)) : 0;
     if (G.lb0 > G.ub0)
       return fail(h, GTD_INVALID_ARG, "graph " + std::to_string(i) + ": seed treedepth below a lower bound");
     levels = std::max(levels, G.ub0 - G.lb0);
@@ -1151,7 +1202,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   if ((s = grow(h, &B.memo, &B.memo_cap, slots * count)) != GTD_OK) return s;
   if ((s = grow(h, &B.i32, &B.i32_cap, 2 * size_t(pool_len) + 2 * size_t(count))) != GTD_OK) return s;
   if ((s = grow(h, &B.u32, &B.u32_cap, size_t(count) * (2 + 2 * size_t(levels)))) != GTD_OK) return s;
-  if ((s = grow(h, &B.i8, &B.i8_cap, size_t(count) * levels * max_n)) != GTD_OK) return s;
+  if ((s = grow(h, &B.i8, &B.i8_cap, 2 * size_t(count) * levels * max_n)) != GTD_OK) return s;
   if ((s = grow(h, &B.u64, &B.u64_cap, 3 * size_t(count) + 1)) != GTD_OK) return s;
   int32_t* d_seed_parent = B.i32;
   int32_t* d_parent = B.i32 + pool_len;
@@ -1176,6 +1227,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   GTD_CUDA(h, cudaMemcpyAsync(d_best, best.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   GTD_CUDA(h, cudaMemcpyAsync(d_lbp, lbp.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   GTD_CUDA(h, cudaMemsetAsync(d_fails, 0, 2 * size_t(count) * levels * sizeof(uint32_t), h->stream));
+  GTD_CUDA(h, cudaMemsetAsync(B.i8 + size_t(count) * levels * max_n, 0, size_t(count) * levels * max_n, h->stream));
   GTD_CUDA(h, cudaMemsetAsync(B.memo, 0, slots * count * sizeof(uint4), h->stream));
   GTD_CUDA(h, cudaMemsetAsync(d_status, 0, count * sizeof(int32_t), h->stream));
   GTD_CUDA(h, cudaMemsetAsync(B.u64, 0, 3 * size_t(count) * sizeof(uint64_t), h->stream));
@@ -1196,6 +1248,9 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   p.fails = d_fails;
   p.claim = d_claim;
   p.lvl_parent = B.i8;
+  p.item_state = reinterpret_cast<uint8_t*>(B.i8 + size_t(count) * levels * max_n);
+  p.unfinished = reinterpret_cast<uint32_t*>(h->d_io + kIoUnfinished);
+  p.window = kRoundWindow;
   p.status = d_status;
   p.t_begin = d_tbeg;
   p.t_end = reinterpret_cast<unsigned long long*>(d_tend);
@@ -1220,8 +1275,30 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   const long long ctas =
       std::max(1ll, std::min<long long>(static_cast<long long>(h->num_sms) * occ, (items + kBnbWarps - 1) / kBnbWarps));
   GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
-  bnb_kernel<<<static_cast<int>(ctas), 32 * kBnbWarps, smem, h->stream>>>(p);
-  GTD_CUDA(h, cudaGetLastError());
+  // Rounds: every item may spend `budget` nodes per launch; the host stops
+  // when every graph is proven or past its deadline.
+  std::vector<uint32_t> rbest(count), rlbp(count);
+  std::vector<int32_t> rstat(count);
+  int32_t rio[4] = {0, 0, 0, 0};
+  p.budget = kFirstBudget;
+  for (int round = 0; round < kMaxRounds; ++round) {
+    GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoTicket, 0, sizeof(int32_t), h->stream));
+    GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoUnfinished, 0, sizeof(int32_t), h->stream));
+    bnb_kernel<<<static_cast<int>(ctas), 32 * kBnbWarps, smem, h->stream>>>(p);
+    GTD_CUDA(h, cudaGetLastError());
+    GTD_CUDA(h, cudaMemcpyAsync(rio, h->d_io, sizeof(rio), cudaMemcpyDeviceToHost, h->stream));
+    GTD_CUDA(h, cudaMemcpyAsync(rbest.data(), d_best, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    GTD_CUDA(h, cudaMemcpyAsync(rlbp.data(), d_lbp, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    GTD_CUDA(h, cudaMemcpyAsync(rstat.data(), d_status, count * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    GTD_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (rio[kIoError] != 0)
+      break;
+    int open = 0;
+    for (int i = 0; i < count; ++i)
+      open += rstat[i] != kBnbTimeout && rlbp[i] < (rbest[i] >> 8);
+    if (open == 0)
+      break;
+  }
   const int tree_ctas = std::min(4096, (count + kBnbWarps - 1) / kBnbWarps);
   bnb_tree_kernel<<<tree_ctas, 32 * kBnbWarps, 0, h->stream>>>(p);
   GTD_CUDA(h, cudaGetLastError());

@@ -465,12 +465,14 @@ def root_accuracy(net: GNN, data: LabelSet) -> dict:
             "td_mae": float(np.concatenate(err).mean()) if err else None, "samples": len(data)}
 
 
-def orders_and_seeds(net: GNN, graphs: Sequence[Graph]):
-    """Branching order (highest score first) and incumbent for each graph:
-    the better of the reference heuristic chain and a greedy elimination by
-    score (gtd_heuristic kind 3)."""
+def guidance(net: GNN, graphs: Sequence[Graph]) -> dict:
+    """What the network gives the branch and bound, per graph: the branching
+    order (highest score first), an incumbent (the better of the reference
+    heuristic chain and a greedy elimination by score, gtd_heuristic kind 3)
+    and a level hint (the rounded td estimate: the decision level tried
+    first). None of it prunes."""
     b = make_batch(graphs)
-    logits, _ = net.forward(b)
+    logits, td_est = net.forward(b)
     orders, seeds = [], []
     for k, g in enumerate(graphs):
         s, e = b.graph_start[k], b.graph_start[k + 1]
@@ -479,4 +481,11 @@ def orders_and_seeds(net: GNN, graphs: Sequence[Graph]):
         t0, p0 = _lib.heuristic(g, 0)
         t1, p1 = _lib.heuristic(g, 3, sc)
         seeds.append((t1, p1) if t1 < t0 else (t0, p0))
-    return orders, seeds
+    hints = np.clip(np.rint(td_est), 1, None).astype(np.int32)
+    return {"orders": orders, "seeds": seeds, "hints": hints, "td_est": td_est}
+
+
+def orders_and_seeds(net: GNN, graphs: Sequence[Graph]):
+    """Branching orders and incumbents only (see guidance)."""
+    gd = guidance(net, graphs)
+    return gd["orders"], gd["seeds"]

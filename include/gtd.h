@@ -181,6 +181,9 @@ typedef struct {
   int memo_log2;        /* memo slots per graph = 2^memo_log2 (0 = sized from free HBM, 2^16..2^24) */
   uint64_t deadline_ns; /* per-graph cap on time-to-proof (0 = 120 s) */
   int ctas_per_sm;      /* 0 = occupancy limit */
+  const int32_t* level_hint; /* per graph, NULL or 0 = none: the decision level
+                                k to try first (e.g. a learned td estimate);
+                                it orders the search and never prunes */
 } gtd_bnb_opts;
 
 typedef struct {

@@ -102,3 +102,12 @@ def test_bnb_unproven_improvements_carry_valid_trees(handle):
     assert np.all(res["td"] <= res["seed_td"])
     for g, t, par in zip(gs, res["td"], res["parents"]):
         assert check_tree(g, t, par), g.name
+
+
+def test_bnb_level_hints_never_change_the_result(handle):
+    gs = _sparse_c3(24, 7) + [G.grid(4, 5), G.cycle(13)]
+    base = _check(handle, gs)
+    rng = np.random.default_rng(5)
+    for hints in (base["td"] + 3, np.maximum(1, base["td"] - 3), rng.integers(1, 12, len(gs)), base["td"]):
+        res = _check(handle, gs, hints=hints.astype(np.int32))
+        assert res["td"].tolist() == base["td"].tolist()
