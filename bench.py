@@ -250,6 +250,9 @@ def measure_dp_c3(h, steps, warmup):
     from gisbdw_gb300.validate import check_tree
     graphs = G.config3_graphs()
     packed = _lib.pack_batch(graphs)
+    t0 = time.perf_counter()
+    rates = h.dp_autotune(10, 24)  # subsets/us per (n, tile bits 8..12); the planner picks from these
+    tune_s = time.perf_counter() - t0
     for _ in range(warmup):
         td, pars, st = h.dp_solve_batch(graphs, packed=packed)
     bad = [g.name for g, t, p in zip(graphs[::64], td[::64], pars[::64]) if not check_tree(g, int(t), p)]
@@ -266,6 +269,7 @@ def measure_dp_c3(h, steps, warmup):
             "alg_GBps": st["alg_bytes"] / (ms / 1e3) / 1e9, "frac_of_" + peak_kind + "_hbm":
             st["alg_bytes"] / (ms / 1e3) / 1e9 / peak, "tile_bits": st["tile_bits"], "ctas": st["ctas"],
             "cuda_graph_replayed": bool(st["graph_replayed"]), "trees_checked": len(graphs[::64]),
+            "autotune_s": tune_s, "autotune_best_bits_n24": int(8 + rates[-1].argmax()),
             "trees_invalid": bad}
 
 
