@@ -341,7 +341,7 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
             "gpu_learned_solved_in_sample": int((learned["status"][:len(sample)] == 0).sum()),
             "gpu_plain_solved_in_sample": int((plain["status"][:len(sample)] == 0).sum()),
             "td_agree": all(r[1] == gpu_td[i] for i, r in enumerate(res) if r[0] == 0 and i in gpu_td),
-            "sample": f"first {len(sample)} config-4 graphs; oracle restatement of BranchAndBound "
+            "sample": f"first {len(sample)} config-{family[1]} graphs; oracle restatement of BranchAndBound "
                       f"(branch_and_bound.cpp:51-114, EdgeLowerBound, HighestDegree(Variance)), "
                       f"{cpu_nodes} nodes per graph, {threads} host threads ({cpu_model()})"}
     return out
