@@ -275,7 +275,7 @@ BNB_MAX_N = 104
 
 class BnbOpts(ctypes.Structure):
     _fields_ = [("memo_log2", ctypes.c_int), ("deadline_ns", ctypes.c_uint64), ("ctas_per_sm", ctypes.c_int),
-                ("level_hint", ctypes.c_void_p)]
+                ("level_hint", ctypes.c_void_p), ("first_budget", ctypes.c_uint32), ("window", ctypes.c_int)]
 
 
 class BnbStats(ctypes.Structure):
@@ -334,7 +334,7 @@ def pack_bnb(graphs, orders=None, seeds=None, seed_kind: int = 0):
 
 
 def _bnb_method(self, graphs, orders=None, seeds=None, memo_log2: int = 0, deadline_ns: int = 0,
-                ctas_per_sm: int = 0, packed=None, hints=None):
+                ctas_per_sm: int = 0, packed=None, hints=None, first_budget: int = 0, window: int = 0):
     """Exact treedepth of every graph by the persistent B&B kernel.
     Returns dict: td, parents, status, proof_ms, nodes, stats."""
     L = _bind_bnb(self.L)
@@ -348,7 +348,8 @@ def _bnb_method(self, graphs, orders=None, seeds=None, memo_log2: int = 0, deadl
     hint_arr = np.ascontiguousarray(hints, dtype=np.int32) if hints is not None else None
     if hint_arr is not None and hint_arr.size != count:
         raise ValueError("one level hint per graph")
-    opts = BnbOpts(memo_log2, deadline_ns, ctas_per_sm, _ptr(hint_arr) if hint_arr is not None else None)
+    opts = BnbOpts(memo_log2, deadline_ns, ctas_per_sm, _ptr(hint_arr) if hint_arr is not None else None,
+                   first_budget, window)
     stats = BnbStats()
     self._check(L.gtd_bnb_solve_batch(self._h, ctypes.cast(descs, _vp), count, _ptr(adj), total,
                                       _ptr(order), _ptr(seed_td), _ptr(seed_par), _ptr(td), _ptr(par),

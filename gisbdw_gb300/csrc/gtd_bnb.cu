@@ -1250,7 +1250,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   p.lvl_parent = B.i8;
   p.item_state = reinterpret_cast<uint8_t*>(B.i8 + size_t(count) * levels * max_n);
   p.unfinished = reinterpret_cast<uint32_t*>(h->d_io + kIoUnfinished);
-  p.window = kRoundWindow;
+  p.window = (opts && opts->window > 0) ? opts->window : kRoundWindow;
   p.status = d_status;
   p.t_begin = d_tbeg;
   p.t_end = reinterpret_cast<unsigned long long*>(d_tend);
@@ -1280,7 +1280,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   std::vector<uint32_t> rbest(count), rlbp(count);
   std::vector<int32_t> rstat(count);
   int32_t rio[4] = {0, 0, 0, 0};
-  p.budget = kFirstBudget;
+  p.budget = (opts && opts->first_budget) ? opts->first_budget : kFirstBudget;
   for (int round = 0; round < kMaxRounds; ++round) {
     GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoTicket, 0, sizeof(int32_t), h->stream));
     GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoUnfinished, 0, sizeof(int32_t), h->stream));

@@ -184,6 +184,8 @@ typedef struct {
   const int32_t* level_hint; /* per graph, NULL or 0 = none: the decision level
                                 k to try first (e.g. a learned td estimate);
                                 it orders the search and never prunes */
+  uint32_t first_budget; /* search nodes of an item's first run per pass (0 = 1024) */
+  int window;            /* decision levels per graph run at a time (0 = 3) */
 } gtd_bnb_opts;
 
 typedef struct {

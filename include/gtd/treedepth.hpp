@@ -217,7 +217,7 @@ class BnBGPU {
     float proof_ms = 0;
     uint64_t nodes = 0;
     parent_.assign(n, -1);
-    gtd_bnb_opts opts{0, deadline_ns_, 0, nullptr};
+    gtd_bnb_opts opts{0, deadline_ns_, 0, nullptr, 0, 0};
     gtd::check(gtd_bnb_solve_batch(handle_.get(), &desc, 1, adj.data(), n, nullptr, &seed_td, seed_parent.data(),
                                    &td, parent_.data(), &status, &proof_ms, &nodes, &opts, &stats_),
                handle_.get());

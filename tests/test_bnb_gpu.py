@@ -111,3 +111,11 @@ def test_bnb_level_hints_never_change_the_result(handle):
     for hints in (base["td"] + 3, np.maximum(1, base["td"] - 3), rng.integers(1, 12, len(gs)), base["td"]):
         res = _check(handle, gs, hints=hints.astype(np.int32))
         assert res["td"].tolist() == base["td"].tolist()
+
+
+def test_bnb_schedule_options_never_change_the_result(handle):
+    gs = _sparse_c3(16, 8) + [G.grid(4, 5)]
+    base = _check(handle, gs)
+    for fb, w in ((64, 1), (256, 2), (1 << 20, 8)):
+        res = _check(handle, gs, first_budget=fb, window=w)
+        assert res["td"].tolist() == base["td"].tolist()
