@@ -90,6 +90,19 @@ def dist_env():
     return rank, world, local
 
 
+def job_rate(units_per_rank, elapsed_s, world):
+    """Whole-job throughput of N replicas: every rank's units over the slowest
+    rank's time (max over ranks by an all-reduce of the process group when
+    world > 1). Returns (rate, slowest elapsed seconds)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(elapsed_s)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_s = float(t.item())
+    return units_per_rank * world / elapsed_s, elapsed_s
+
+
 def peaks():
     try:
         with open(PEAKS_PATH) as f:
@@ -405,12 +418,8 @@ def run_gpu(args, graphs):
     barrier()
     elapsed_ms = ev0.elapsed_time(ev1)
     clocks = sampler.stop()
-    if world > 1:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    solves = len(graphs) * args.steps * world
-    value = solves / (elapsed_ms / 1000.0)
+    value, elapsed_s = job_rate(len(graphs) * args.steps, elapsed_ms / 1000.0, world)
+    elapsed_ms = elapsed_s * 1000.0
 
     # e2e: host buffers through the C ABI call (adjacency H2D, results D2H)
     e2e_times = []
@@ -427,7 +436,7 @@ def run_gpu(args, graphs):
             td, par, order, _ = h.dp_solve(adjs[i], g.n, tile_bits=args.tile_bits)
     e2e_s = time.perf_counter() - t0
     barrier()
-    e2e_value = len(graphs) * args.steps * world / e2e_s
+    e2e_value, _ = job_rate(len(graphs) * args.steps, e2e_s, world)
 
     # roofline of the dominant kernel (dp_tile_kernel), from live events
     alg = sum(s["alg_bytes"] for s in kstats)
