@@ -119,3 +119,16 @@ def test_bnb_schedule_options_never_change_the_result(handle):
     for fb, w in ((64, 1), (256, 2), (1 << 20, 8)):
         res = _check(handle, gs, first_budget=fb, window=w)
         assert res["td"].tolist() == base["td"].tolist()
+
+
+def test_bnb_graphs_wider_than_64_vertices(handle):
+    # closed forms: td(P_n) = ceil(log2(n + 1)), td(C_n) = 1 + ceil(log2(n)), td(star) = 2
+    gs = [G.path(65), G.path(100), G.cycle(70), G.cycle(90), G.star(104)]
+    res = _check(handle, gs)
+    assert res["td"].tolist() == [7, 7, 8, 8, 2]
+    # sparse graphs using both mask words: any result must carry a valid tree
+    rs = [G.tree_plus_edges(n, k, s) for n, k, s in ((70, 0, 1), (90, 2, 2), (104, 3, 3))]
+    r2 = handle.bnb_solve_batch(rs, deadline_ns=20 * 10**9)
+    assert set(r2["status"].tolist()) <= {0, 4}
+    for g, t, par in zip(rs, r2["td"], r2["parents"]):
+        assert check_tree(g, t, par), g.name
