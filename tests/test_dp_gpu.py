@@ -117,6 +117,20 @@ def test_dp_config2_sized_properties(handle, port):
     assert stats["dp_ms"] > 0
 
 
+@pytest.mark.parametrize("n", [34, 36])
+def test_dp_maximum_sizes(handle, port, n):
+    """The largest tables (16 and 64 GiB): the same size-independent facts on
+    a sparse random graph, and closed forms at the maximum n."""
+    g = G.gnp_connected(n, 0.12, 7)
+    td, parent, order, _ = handle.dp_solve(g.adj64(), g.n)
+    assert port.check_valid(g, td, parent)
+    etd, epar = port.elimination_tree(g, order)
+    assert etd == td and epar.tolist() == parent.tolist()
+    assert port.edge_lower_bound(g.n, g.m) <= td <= port.heuristic(g, 0)[0]
+    assert handle.dp_solve(G.path(n).adj64(), n)[0] == math.ceil(math.log2(n + 1))
+    assert handle.dp_solve(G.cycle(n).adj64(), n)[0] == 1 + math.ceil(math.log2(n))
+
+
 def test_dp_closed_forms(handle):
     for n in (3, 7, 15, 16, 31, 32):
         assert handle.dp_solve(G.path(n).adj64(), n)[0] == math.ceil(math.log2(n + 1))
