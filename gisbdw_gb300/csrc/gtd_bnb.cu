@@ -104,6 +104,7 @@ struct BnbParams {
   uint8_t* item_state = nullptr;   // per graph x level x rank: kItemDone, or the item's budget doublings so far
   uint64_t budget = 0;             // an item's first budget in search nodes (0 = unlimited)
   int window = 0;                  // levels run at a time below a graph's top level (0 = all)
+  int split = 0;                   // 1: an item is a pair (first root, second root)
   uint32_t* unfinished = nullptr;  // items that used up their budget this round
   int8_t* lvl_parent = nullptr;    // per graph x level: tree (max_n entries, -1 root)
   int32_t* status = nullptr;       // per graph BnbStatus
@@ -764,13 +765,21 @@ struct Search {
   // component left is decided again at the depth it needs, which the memo
   // entries written by the accepting search answer at once (a search only
   // where an entry has been evicted). parent_out[u] (int8, -1 at the root)
-  // for u in C. False if a component fails (an error), or on a stop.
-  __device__ bool build_tree(uint64_t Clo, uint64_t Chi, int k, int root, int8_t* parent_out) {
-    if (lane == 0)
+  // for u in C. With root2 >= 0 (C - root connected), root2 is fixed as
+  // root's only child. False if a component fails (an error), or on a stop.
+  __device__ bool build_tree(uint64_t Clo, uint64_t Chi, int k, int root, int8_t* parent_out, int root2 = -1) {
+    if (lane == 0) {
       parent_out[root] = -1;
+      if (root2 >= 0)
+        parent_out[root2] = static_cast<int8_t>(root);
+    }
     int top = 0;
     uint64_t rlo = Clo, rhi = Chi;
     bit_clear(rlo, rhi, root);
+    const int owner0 = root2 >= 0 ? root2 : root;
+    const int k0 = root2 >= 0 ? k - 2 : k - 1;
+    if (root2 >= 0)
+      bit_clear(rlo, rhi, root2);
     while (rlo | rhi) {
       uint64_t clo, chi;
       component(rlo, rhi, first128(rlo, rhi), clo, chi);
@@ -779,9 +788,9 @@ struct Search {
       if (lane == 0) {
         w->qlo[top] = clo;
         w->qhi[top] = chi;
-        w->qown[top] = static_cast<uint8_t>(root);
-        w->qk[top] = static_cast<uint8_t>(k - 1);
-        w->qdep[top] = 2;
+        w->qown[top] = static_cast<uint8_t>(owner0);
+        w->qk[top] = static_cast<uint8_t>(k0);
+        w->qdep[top] = static_cast<uint8_t>(root2 >= 0 ? 3 : 2);
       }
       ++top;
     }
@@ -845,7 +854,8 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   WarpMem* w = reinterpret_cast<WarpMem*>(smem) + warp;
   int cur_g = -1;
-  const uint32_t per_level = static_cast<uint32_t>(p.max_n) * static_cast<uint32_t>(p.num_graphs);
+  const uint32_t S = p.split ? static_cast<uint32_t>(p.max_n) : 1u;  // second roots per first root
+  const uint32_t per_level = static_cast<uint32_t>(p.max_n) * S * static_cast<uint32_t>(p.num_graphs);
   const uint32_t total = per_level * static_cast<uint32_t>(p.levels);
   for (;;) {
     uint32_t item = 0;
@@ -856,13 +866,14 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
       break;
     const int li = static_cast<int>(item / per_level);
     const uint32_t rem = item % per_level;
-    const int r = static_cast<int>(rem / p.num_graphs);
+    const uint32_t rr = rem / p.num_graphs;
     const int g = static_cast<int>(rem % p.num_graphs);
+    const int r = static_cast<int>(rr / S), r2 = static_cast<int>(rr % S);
     const BnbGraph G = p.graphs[g];
     const int k = G.ub0 - 1 - li;
-    if (r >= G.n || k < G.lb0)
+    if (r >= G.n || r2 >= (p.split ? G.n : 1) || k < G.lb0)
       continue;
-    const size_t item_idx = (size_t(g) * p.levels + li) * p.max_n + r;
+    const size_t item_idx = ((size_t(g) * p.levels + li) * p.max_n + r) * S + r2;
     const uint32_t istate = p.item_state[item_idx];
     if (istate == kItemDone)
       continue;  // finished in an earlier round
@@ -908,9 +919,34 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
       s.stop.deadline = __shfl_sync(0xffffffffu, b, 0) + p.deadline_ns;
     }
     bool ok = false;
+    int u = -1;  // fixed second root (split items)
     const bool skip = G.n >= 3 && s.dominated(v, fl, fh);  // another root is at least as good
-    if (!skip)
+    if (!skip && !p.split) {
       ok = s.decide(fl, fh, k, v, nullptr);
+    } else if (!skip) {
+      // Split item (v, order[r2]): when C - v is connected, decide C - v under
+      // root u at depth k - 1; else item r2 = 0 decides all of v and the
+      // others have nothing to do (they count as failed).
+      uint64_t cl = fl, ch = fh;
+      bit_clear(cl, ch, v);
+      bool conn = false;
+      if (G.n >= 3) {
+        uint64_t dl, dh;
+        s.component(cl, ch, first128(cl, ch), dl, dh);
+        conn = dl == cl && dh == ch;
+      }
+      if (!conn) {
+        if (r2 == 0)
+          ok = s.decide(fl, fh, k, v, nullptr);
+      } else {
+        const int cand = w->order[r2];
+        // u = v, or u dominated as a root of C - v: another second root is at least as good
+        if (cand != v && !(G.n - 1 >= 3 && s.dominated(cand, cl, ch))) {
+          ok = s.decide(cl, ch, k - 1, cand, nullptr);
+          u = cand;
+        }
+      }
+    }
     // A success is published only with its tree: the first success of a
     // level claims the level's parent buffer and builds the tree while the
     // memo entries of its search are fresh; later successes of the level
@@ -924,7 +960,7 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
       if (claimed) {
         int8_t* tree = p.lvl_parent + (size_t(g) * p.levels + li) * p.max_n;
         s.stop.budget = 0;  // the tree is mostly memo hits: no yield half way
-        publish = s.build_tree(fl, fh, k, v, tree);
+        publish = s.build_tree(fl, fh, k, v, tree, ok ? u : -1);
         if (!publish && !s.timed_out && !s.cancelled && lane == 0)
           raise_error(p.error, kDevNoRoot, g);
         __threadfence();
@@ -944,7 +980,8 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
         if (ok) {
           if (publish)
             atomicMin(p.best + g, (static_cast<uint32_t>(k) << 8) | static_cast<uint32_t>(v));
-        } else if (atomicAdd(p.fails + size_t(g) * p.levels + li, 1u) + 1 == static_cast<uint32_t>(G.n)) {
+        } else if (atomicAdd(p.fails + size_t(g) * p.levels + li, 1u) + 1 ==
+                   static_cast<uint32_t>(p.split ? G.n * G.n : G.n)) {
           atomicMax(p.lbp + g, static_cast<uint32_t>(k + 1));  // every root failed: td > k
         }
         check_proved(p, g);
@@ -1202,7 +1239,15 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   if ((s = grow(h, &B.memo, &B.memo_cap, slots * count)) != GTD_OK) return s;
   if ((s = grow(h, &B.i32, &B.i32_cap, 2 * size_t(pool_len) + 2 * size_t(count))) != GTD_OK) return s;
   if ((s = grow(h, &B.u32, &B.u32_cap, size_t(count) * (2 + 2 * size_t(levels)))) != GTD_OK) return s;
-  if ((s = grow(h, &B.i8, &B.i8_cap, 2 * size_t(count) * levels * max_n)) != GTD_OK) return s;
+  // Split items (first root x second root) when the batch is too small to
+  // give every warp a first-root item: a single graph then uses n^2 warps.
+  size_t first_items = 0;
+  for (int i = 0; i < count; ++i)
+    first_items += size_t(descs[i].n) * std::min(levels, kRoundWindow);
+  const int split = (first_items < size_t(h->num_sms) * 16 &&
+                     size_t(count) * levels * max_n * max_n < (size_t(1) << 31)) ? 1 : 0;
+  const size_t S = split ? size_t(max_n) : 1;
+  if ((s = grow(h, &B.i8, &B.i8_cap, size_t(count) * levels * max_n * (1 + S))) != GTD_OK) return s;
   if ((s = grow(h, &B.u64, &B.u64_cap, 3 * size_t(count) + 1)) != GTD_OK) return s;
   int32_t* d_seed_parent = B.i32;
   int32_t* d_parent = B.i32 + pool_len;
@@ -1227,7 +1272,8 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   GTD_CUDA(h, cudaMemcpyAsync(d_best, best.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   GTD_CUDA(h, cudaMemcpyAsync(d_lbp, lbp.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
   GTD_CUDA(h, cudaMemsetAsync(d_fails, 0, 2 * size_t(count) * levels * sizeof(uint32_t), h->stream));
-  GTD_CUDA(h, cudaMemsetAsync(B.i8 + size_t(count) * levels * max_n, 0, size_t(count) * levels * max_n, h->stream));
+  GTD_CUDA(h, cudaMemsetAsync(B.i8 + size_t(count) * levels * max_n, 0, size_t(count) * levels * max_n * S,
+                              h->stream));
   GTD_CUDA(h, cudaMemsetAsync(B.memo, 0, slots * count * sizeof(uint4), h->stream));
   GTD_CUDA(h, cudaMemsetAsync(d_status, 0, count * sizeof(int32_t), h->stream));
   GTD_CUDA(h, cudaMemsetAsync(B.u64, 0, 3 * size_t(count) * sizeof(uint64_t), h->stream));
@@ -1249,6 +1295,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   p.claim = d_claim;
   p.lvl_parent = B.i8;
   p.item_state = reinterpret_cast<uint8_t*>(B.i8 + size_t(count) * levels * max_n);
+  p.split = split;
   p.unfinished = reinterpret_cast<uint32_t*>(h->d_io + kIoUnfinished);
   p.window = (opts && opts->window > 0) ? opts->window : kRoundWindow;
   p.status = d_status;
@@ -1271,7 +1318,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
     occ = opts->ctas_per_sm;
   if (occ < 1)
     occ = 1;
-  const long long items = static_cast<long long>(count) * max_n * levels;
+  const long long items = static_cast<long long>(count) * max_n * levels * static_cast<long long>(S);
   const long long ctas =
       std::max(1ll, std::min<long long>(static_cast<long long>(h->num_sms) * occ, (items + kBnbWarps - 1) / kBnbWarps));
   GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
