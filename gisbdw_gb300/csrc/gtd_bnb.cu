@@ -70,6 +70,7 @@ constexpr int kMmdMin = 10;              // minor-min-width bound for |C| >= thi
 constexpr uint32_t kSeedRoot = 0xFFu;
 constexpr int kUnknownUb = 127;
 constexpr int kIoUnfinished = 3;         // d_io word: items that spent their budget this round
+constexpr int kIoExited = 200;           // d_io word: warps that left the current pass
 constexpr uint64_t kFirstBudget = 1024;  // search nodes of an item's first run
 constexpr uint32_t kMaxDoublings = 30;   // an item's budget grows to at most 2^30 times the first
 constexpr uint32_t kItemDone = 0xFF;
@@ -106,6 +107,9 @@ struct BnbParams {
   int window = 0;                  // levels run at a time below a graph's top level (0 = all)
   int split = 0;                   // 1: an item is a pair (first root, second root)
   uint32_t* unfinished = nullptr;  // items that used up their budget this round
+  uint32_t* exited = nullptr;      // [0] warps that found no ticket left, [1] items started (this pass)
+  uint32_t drain_at = 0;           // running items yield once this many warps have left
+  uint32_t full_at = 0;            // ... and at least this many items have started
   int8_t* lvl_parent = nullptr;    // per graph x level: tree (max_n entries, -1 root)
   int32_t* status = nullptr;       // per graph BnbStatus
   uint64_t* t_begin = nullptr;     // per graph: first item start (globaltimer ns)
@@ -278,6 +282,9 @@ struct StopCheck {
   int item_k = 0;
   uint64_t deadline = 0;           // absolute ns, 0 = none
   uint64_t budget = 0;             // nodes before the item yields, 0 = none
+  const uint32_t* exited = nullptr; // warps that left this pass, items started in it:
+  uint32_t drain_at = 0;            // a pass that started at least one item per warp
+  uint32_t full_at = 0;             // drains once half of its warps have left
 };
 
 struct Search {
@@ -567,8 +574,10 @@ struct Search {
     if (lane == 0) {
       if (stop.deadline && global_ns() > stop.deadline)
         flag = 1;
-      else if (stop.budget && nodes >= stop.budget)
-        flag = 3;
+      else if (stop.budget && (nodes >= stop.budget ||
+                               (stop.exited && ld_acquire_u32(stop.exited) >= stop.drain_at &&
+                                ld_acquire_u32(stop.exited + 1) >= stop.full_at)))
+        flag = 3;  // budget spent, or the pass is draining: back next pass with twice the budget
       else if ((stop.best && static_cast<int>(ld_acquire_u32(stop.best) >> 8) <= stop.item_k) ||
                (stop.lbp && static_cast<int>(ld_acquire_u32(stop.lbp)) > stop.item_k))
         flag = 2;
@@ -862,8 +871,11 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
     if (lane == 0)
       item = ld_relaxed_s32(p.error) != 0 ? 0xffffffffu : atomicAdd(p.ticket, 1u);
     item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= total)
+    if (item >= total) {
+      if (lane == 0 && p.exited)
+        atomicAdd(p.exited, 1u);
       break;
+    }
     const int li = static_cast<int>(item / per_level);
     const uint32_t rem = item % per_level;
     const uint32_t rr = rem / p.num_graphs;
@@ -912,6 +924,11 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
     s.stop.lbp = p.lbp + g;
     s.stop.item_k = k;
     s.stop.budget = p.budget ? (p.budget << istate) : 0;
+    s.stop.exited = p.exited;
+    s.stop.drain_at = p.drain_at;
+    s.stop.full_at = p.full_at;
+    if (lane == 0 && p.exited)
+      atomicAdd(p.exited + 1, 1u);
     if (p.deadline_ns) {
       uint64_t b = 0;
       if (lane == 0)
@@ -959,7 +976,7 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_con
       claimed = __shfl_sync(0xffffffffu, claimed, 0);
       if (claimed) {
         int8_t* tree = p.lvl_parent + (size_t(g) * p.levels + li) * p.max_n;
-        s.stop.budget = 0;  // the tree is mostly memo hits: no yield half way
+        s.stop.budget = 0;  // the tree is mostly memo hits: no yield half way (nor a drain)
         publish = s.build_tree(fl, fh, k, v, tree, ok ? u : -1);
         if (!publish && !s.timed_out && !s.cancelled && lane == 0)
           raise_error(p.error, kDevNoRoot, g);
@@ -1297,6 +1314,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   p.item_state = reinterpret_cast<uint8_t*>(B.i8 + size_t(count) * levels * max_n);
   p.split = split;
   p.unfinished = reinterpret_cast<uint32_t*>(h->d_io + kIoUnfinished);
+  p.exited = reinterpret_cast<uint32_t*>(h->d_io + kIoExited);
   p.window = (opts && opts->window > 0) ? opts->window : kRoundWindow;
   p.status = d_status;
   p.t_begin = d_tbeg;
@@ -1321,6 +1339,8 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   const long long items = static_cast<long long>(count) * max_n * levels * static_cast<long long>(S);
   const long long ctas =
       std::max(1ll, std::min<long long>(static_cast<long long>(h->num_sms) * occ, (items + kBnbWarps - 1) / kBnbWarps));
+  p.drain_at = static_cast<uint32_t>(std::max(1ll, ctas * kBnbWarps / 2));
+  p.full_at = static_cast<uint32_t>(ctas * kBnbWarps);
   GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
   // Rounds: every item may spend `budget` nodes per launch; the host stops
   // when every graph is proven or past its deadline.
@@ -1331,6 +1351,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   for (int round = 0; round < kMaxRounds; ++round) {
     GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoTicket, 0, sizeof(int32_t), h->stream));
     GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoUnfinished, 0, sizeof(int32_t), h->stream));
+    GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoExited, 0, 2 * sizeof(int32_t), h->stream));
     bnb_kernel<<<static_cast<int>(ctas), 32 * kBnbWarps, smem, h->stream>>>(p);
     GTD_CUDA(h, cudaGetLastError());
     GTD_CUDA(h, cudaMemcpyAsync(rio, h->d_io, sizeof(rio), cudaMemcpyDeviceToHost, h->stream));
