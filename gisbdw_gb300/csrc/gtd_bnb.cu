@@ -22,12 +22,12 @@
 //    (edge_lower_bound.hpp:13-20: smallest d with (d-1)(2n-d) >= 2e), a
 //    minor-min-width treewidth bound (td >= tw + 1), a longest-path bound
 //    (td >= ceil(log2(L + 1)) for a greedy path of L vertices, one walk per
-//    lane, tried when 2^k <= |C|), root domination (u is
-//    not tried as a root when N(u) lies in N[v] for a v of larger degree or
-//    equal degree and smaller id: v is at least as good), and a per-graph memo in HBM of a lower and an
-//    upper bound (with a root achieving it) per component, keyed by the
-//    component's vertex mask in 128-bit slots updated by atomic CAS and
-//    shared by every warp working on that graph.
+//    lane, tried when 2^k <= |C|), root domination (u is not tried as a
+//    root when N(u) lies in N[v] for a v of larger degree or equal degree
+//    and smaller id: v is at least as good), and a per-graph memo in HBM of
+//    a lower and an upper bound (with a root achieving it) per component,
+//    keyed by the component's vertex mask in 128-bit slots updated by
+//    atomic CAS and shared by every warp working on that graph.
 //  * Schedule: persistent launches over a global atomic queue of items
 //    (graph, level k, root candidate), issued for k descending from the
 //    incumbent minus one, candidates in priority order, graphs interleaved.
@@ -39,7 +39,13 @@
 //    into [proven lower bound, best - 1] (the learned td estimate: it orders
 //    which decisions run first and never prunes; a wrong hint only moves the
 //    window). Easy graphs finish in the first passes instead of waiting
-//    behind the long items of hard graphs.
+//    behind the long items of hard graphs. A pass that started at least one
+//    item per warp drains once half of its warps found no ticket left: the
+//    items still running yield as if their budget were spent.
+//    Split items: when a batch has fewer first-root items than the GPU has
+//    warps, an item is a pair (first root v, second root u) deciding C - v
+//    under root u at depth k - 1 (C - v connected; else the u = 0 item
+//    decides all of v), so a single graph uses n^2 warps.
 //    A success at level k improves the graph's best (atomicMin) and
 //    cancels every remaining item at levels >= k; when every candidate at
 //    level k has failed, the graph's proven lower bound becomes k + 1 and
