@@ -864,7 +864,7 @@ __device__ __forceinline__ void check_proved(const BnbParams& p, int g) {
     atomicCAS(p.t_end + g, 0ull, static_cast<unsigned long long>(global_ns()));
 }
 
-__global__ void __launch_bounds__(32 * kBnbWarps, 4) bnb_kernel(const __grid_constant__ BnbParams p) {
+__global__ void __launch_bounds__(32 * kBnbWarps, 6) bnb_kernel(const __grid_constant__ BnbParams p) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   WarpMem* w = reinterpret_cast<WarpMem*>(smem) + warp;
