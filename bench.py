@@ -326,6 +326,8 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
                 "p50_proof_ms_capped": float(np.median(np.where(ok, pm, cap_s * 1e3))),
                 "p99_proof_ms_capped": float(np.percentile(np.where(ok, pm, cap_s * 1e3), 99)),
                 "nodes": int(res["nodes"].sum()), "batch_ms": res["stats"]["ms"], "by_family": fam,
+                "nodes_per_s": float(res["nodes"].sum() / (res["stats"]["ms"] / 1e3)),
+                "p50_nodes_per_proven_graph": float(np.median(res["nodes"][ok])) if ok.any() else None,
                 "trees_valid": all(check_tree(g, int(t), par) for g, t, par in
                                    zip(graphs, res["td"], res["parents"]))}
     ps, ls = summary(plain), summary(learned, t_inf)
