@@ -73,6 +73,7 @@ constexpr int kBnbWarps = 4;
 constexpr int kMaxComps = 40;            // components with >= 3 vertices: <= 104 / 3
 constexpr int kMemoProbes = 8;
 constexpr int kMmdMin = 10;              // minor-min-width bound for |C| >= this
+constexpr int kSubsetMin = 16;           // memo bounds of the C - v for |C| >= this
 constexpr uint32_t kSeedRoot = 0xFFu;
 constexpr int kUnknownUb = 127;
 constexpr int kIoUnfinished = 3;         // d_io word: items that spent their budget this round
@@ -405,6 +406,22 @@ struct Search {
     return 32 - __clz(static_cast<int>(len));
   }
 
+  // Largest memo lower bound over the vertex-deleted subsets C - v (one
+  // lookup per vertex, lanes in parallel); 0 where nothing is known.
+  __device__ int subset_lb(uint64_t Clo, uint64_t Chi) const {
+    int best = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int v = lane + 32 * k;
+      if (v < n && has(Clo, Chi, v)) {
+        uint64_t lo = Clo, hi = Chi;
+        bit_clear(lo, hi, v);
+        best = max(best, memo_get(memo, memo_mask, lo, hi).lb);
+      }
+    }
+    return static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<uint32_t>(best)));
+  }
+
   // Root domination (per lane, no warp collectives). If N_C(u) is contained
   // in N_C[v] for some v != u in C, swapping u and v in any elimination tree
   // of C rooted at u gives a valid tree of the same height rooted at v (v's
@@ -661,6 +678,16 @@ struct Search {
                 const int pl = path_lb(f.lo, f.hi, 1 << fk);
                 if (pl > fk) {
                   lb = pl;
+                  if (lane == 0)
+                    memo_put(memo, memo_mask, f.lo, f.hi, lb, kUnknownUb, 0);
+                }
+              }
+              // td is monotone under vertex deletion: a memo entry proving
+              // td(C - v) > fk for any v refutes td(C) <= fk at once
+              if (lb <= fk && csize >= kSubsetMin) {
+                const int sl = subset_lb(f.lo, f.hi);
+                if (sl > fk) {
+                  lb = sl;
                   if (lane == 0)
                     memo_put(memo, memo_mask, f.lo, f.hi, lb, kUnknownUb, 0);
                 }
