@@ -406,19 +406,26 @@ struct Search {
     return 32 - __clz(static_cast<int>(len));
   }
 
-  // Largest memo lower bound over the vertex-deleted subsets C - v (one
-  // lookup per vertex, lanes in parallel); 0 where nothing is known.
-  __device__ int subset_lb(uint64_t Clo, uint64_t Chi) const {
+  // Memo bounds of the vertex-deleted subsets C - v (one lookup per vertex,
+  // lanes in parallel): the largest lower bound (0 where nothing is known)
+  // and, in *ub_root, (smallest upper bound << 8 | its v). Memo keys are
+  // components, so a hit on C - v means C - v is connected.
+  __device__ int subset_bounds(uint64_t Clo, uint64_t Chi, uint32_t* ub_root) const {
     int best = 0;
+    uint32_t ubr = 0xFFFFFFFFu;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int v = lane + 32 * k;
       if (v < n && has(Clo, Chi, v)) {
         uint64_t lo = Clo, hi = Chi;
         bit_clear(lo, hi, v);
-        best = max(best, memo_get(memo, memo_mask, lo, hi).lb);
+        const MemoHit m = memo_get(memo, memo_mask, lo, hi);
+        best = max(best, m.lb);
+        if (m.ub < kUnknownUb)
+          ubr = min(ubr, (static_cast<uint32_t>(m.ub) << 8) | static_cast<uint32_t>(v));
       }
     }
+    *ub_root = __reduce_min_sync(0xffffffffu, ubr);
     return static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<uint32_t>(best)));
   }
 
@@ -683,17 +690,25 @@ struct Search {
                 }
               }
               // td is monotone under vertex deletion: a memo entry proving
-              // td(C - v) > fk for any v refutes td(C) <= fk at once
+              // td(C - v) > fk for any v refutes td(C) <= fk at once; one
+              // proving td(C - v) <= fk - 1 (C - v connected) accepts root v
+              uint32_t ubr = 0xFFFFFFFFu;
               if (lb <= fk && csize >= kSubsetMin) {
-                const int sl = subset_lb(f.lo, f.hi);
+                const int sl = subset_bounds(f.lo, f.hi, &ubr);
                 if (sl > fk) {
                   lb = sl;
                   if (lane == 0)
                     memo_put(memo, memo_mask, f.lo, f.hi, lb, kUnknownUb, 0);
                 }
               }
-              if (lb > fk)
+              if (lb > fk) {
                 verdict = 0;
+              } else if (ubr != 0xFFFFFFFFu && static_cast<int>(ubr >> 8) <= fk - 1) {
+                verdict = 1;
+                vroot = static_cast<int>(ubr & 0xFF);
+                if (lane == 0)
+                  memo_put(memo, memo_mask, f.lo, f.hi, 0, fk, vroot);
+              }
             }
           }
         }
