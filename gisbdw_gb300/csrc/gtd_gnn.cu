@@ -118,9 +118,11 @@ __global__ void node_linear_t(int N, int K, int H, const float* __restrict__ dZ,
   }
 }
 
-// dW += X^T dZ over a chunk of 64 nodes per block; db += column sums of dZ.
+// Partial X^T dZ (and column sums of dZ) of a chunk of 64 nodes per block,
+// written to part[block][K * H + H]; reduce_partials adds the chunks in a
+// fixed order, so the gradient (and training) is deterministic.
 __global__ void weight_grad(int N, int K, int H, const float* __restrict__ X, const float* __restrict__ dZ,
-                            float* __restrict__ dW, float* __restrict__ db) {
+                            float* __restrict__ part) {
   constexpr int kChunk = 64;
   __shared__ float xs[kChunk][kMaxK], ds[kChunk][kMaxK];
   const int v0 = blockIdx.x * kChunk;
@@ -131,20 +133,35 @@ __global__ void weight_grad(int N, int K, int H, const float* __restrict__ X, co
     ds[r][c] = (r < nv && c < H) ? dZ[size_t(v0 + r) * H + c] : 0.f;
   }
   __syncthreads();
+  float* out = part + size_t(blockIdx.x) * (K * H + H);
   for (int t = threadIdx.x; t < K * H; t += blockDim.x) {
     const int i = t / H, j = t % H;
     float acc = 0.f;
     for (int r = 0; r < nv; ++r)
       acc = fmaf(xs[r][i], ds[r][j], acc);
-    atomicAdd(dW + t, acc);
+    out[t] = acc;
   }
-  if (db)
-    for (int j = threadIdx.x; j < H; j += blockDim.x) {
-      float acc = 0.f;
-      for (int r = 0; r < nv; ++r)
-        acc += ds[r][j];
-      atomicAdd(db + j, acc);
-    }
+  for (int j = threadIdx.x; j < H; j += blockDim.x) {
+    float acc = 0.f;
+    for (int r = 0; r < nv; ++r)
+      acc += ds[r][j];
+    out[K * H + j] = acc;
+  }
+}
+
+// dW += sum over chunks of the partials, db likewise (when non-null).
+__global__ void reduce_partials(int chunks, int KH, int H, const float* __restrict__ part, float* __restrict__ dW,
+                                float* __restrict__ db) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= KH + H || (t >= KH && !db))
+    return;
+  float acc = 0.f;
+  for (int c = 0; c < chunks; ++c)
+    acc += part[size_t(c) * (KH + H) + t];
+  if (t < KH)
+    dW[t] += acc;
+  else
+    db[t - KH] += acc;
 }
 
 // a(v) = mean over neighbours of h(u); one thread per (v, channel).
@@ -327,6 +344,7 @@ struct Views {
   float *Z, *Hs, *A;  // (L + 1) x N x H, (L + 1) x N x H, L x N x H
   float *logits, *pooled, *td_est, *loss;
   float *dh, *dz, *da, *tmp, *dlogit, *dtd;
+  float* part;  // weight-gradient partials, one row per 64-node chunk
 };
 
 gtd_status prepare(gtd_gnn g, const gtd_gnn_batch* b, bool train, Views& V) {
@@ -345,7 +363,8 @@ gtd_status prepare(gtd_gnn g, const gtd_gnn_batch* b, bool train, Views& V) {
                oZ = take((L + 1) * N * H * 4), oH = take((L + 1) * N * H * 4), oA = take(L * N * H * 4),
                olog = take(N * 4), opool = take(G * H * 4), otde = take(G * 4), oloss = take(4), odh = take(N * H * 4),
                odz = take(N * H * 4), oda = take(N * H * 4), otmp = take(N * H * 4), odl = take(N * 4),
-               odt = take(G * 4);
+               odt = take(G * 4),
+               opart = take(((std::max(N, G) + 63) / 64) * (size_t(std::max(g->fin, g->hid)) * H + H) * 4);
   GTD_CUDA(h, gtd::ensure_device(&g->buf, &g->buf_cap, off));
   char* base = static_cast<char*>(g->buf);
   V.x = reinterpret_cast<float*>(base + ox);
@@ -369,6 +388,7 @@ gtd_status prepare(gtd_gnn g, const gtd_gnn_batch* b, bool train, Views& V) {
   V.tmp = reinterpret_cast<float*>(base + otmp);
   V.dlogit = reinterpret_cast<float*>(base + odl);
   V.dtd = reinterpret_cast<float*>(base + odt);
+  V.part = reinterpret_cast<float*>(base + opart);
   cudaStream_t s = h->stream;
   GTD_CUDA(h, cudaMemcpyAsync(V.x, b->x, N * g->fin * 4, cudaMemcpyHostToDevice, s));
   GTD_CUDA(h, cudaMemcpyAsync(V.gstart, b->graph_start, (G + 1) * 4, cudaMemcpyHostToDevice, s));
@@ -414,6 +434,15 @@ gtd_status forward(gtd_gnn g, const gtd_gnn_batch* b, const Views& V) {
   return GTD_OK;
 }
 
+// Weight gradient of one linear map over N rows: per-chunk partials, then
+// their ordered sum into dW (and db).
+void wgrad(cudaStream_t s, int N, int K, int H, const float* X, const float* dZ, float* dW, float* db, float* part) {
+  const unsigned chunks = gtd::blocks_for(size_t(N), 64);
+  gtd::weight_grad<<<chunks, 256, 0, s>>>(N, K, H, X, dZ, part);
+  gtd::reduce_partials<<<gtd::blocks_for(size_t(K) * H + H, 256), 256, 0, s>>>(static_cast<int>(chunks), K * H, H,
+                                                                              part, dW, db);
+}
+
 gtd_status backward(gtd_gnn g, const gtd_gnn_batch* b, const Views& V, float td_weight) {
   gtd_handle h = g->h;
   const int N = b->num_nodes, G = b->num_graphs, H = g->hid, L = g->layers;
@@ -431,19 +460,16 @@ gtd_status backward(gtd_gnn g, const gtd_gnn_batch* b, const Views& V, float td_
       N, G, H, V.gstart, V.graph_of, V.logits, V.td_est, V.y, V.mask, V.td_label, inv, td_weight, g->w + P.head,
       g->w + P.head + H + 1, V.dlogit, V.dtd, V.dh, V.loss);
   // w_out, b_out from h_L and dlogit; w_g, b_g from the pooled means and dtd
-  gtd::weight_grad<<<gtd::blocks_for(size_t(N), 64), 256, 0, s>>>(N, H, 1, V.Hs + L * NH, V.dlogit, gr + P.head,
-                                                                   gr + P.head + H);
-  gtd::weight_grad<<<gtd::blocks_for(size_t(G), 64), 256, 0, s>>>(G, H, 1, V.pooled, V.dtd, gr + P.head + H + 1,
-                                                                   gr + P.head + 2 * H + 1);
+  wgrad(s, N, H, 1, V.Hs + L * NH, V.dlogit, gr + P.head, gr + P.head + H, V.part);
+  wgrad(s, G, H, 1, V.pooled, V.dtd, gr + P.head + H + 1, gr + P.head + 2 * H + 1, V.part);
   GTD_CUDA(h, cudaGetLastError());
   const unsigned nb = gtd::blocks_for(size_t(N), gtd::kNodesPerBlock);
-  const unsigned cb = gtd::blocks_for(size_t(N), 64);
   const unsigned eb = gtd::blocks_for(NH, 256);
   for (int l = L - 1; l >= 0; --l) {
     // dz = dh * relu'(z_{l+1})
     gtd::relu_mask<<<eb, 256, 0, s>>>(NH, V.Z + (l + 1) * NH, V.dh, V.dz);
-    gtd::weight_grad<<<cb, 256, 0, s>>>(N, H, H, V.Hs + l * NH, V.dz, gr + P.ws(l, H), gr + P.b(l, H));
-    gtd::weight_grad<<<cb, 256, 0, s>>>(N, H, H, V.A + l * NH, V.dz, gr + P.wn(l, H), nullptr);
+    wgrad(s, N, H, H, V.Hs + l * NH, V.dz, gr + P.ws(l, H), gr + P.b(l, H), V.part);
+    wgrad(s, N, H, H, V.A + l * NH, V.dz, gr + P.wn(l, H), nullptr, V.part);
     // dh_l = dz Ws^T + aggregate^T(dz Wn^T)
     gtd::node_linear_t<<<nb, 64, 0, s>>>(N, H, H, V.dz, g->w + P.wn(l, H), V.da);
     gtd::node_linear_t<<<nb, 64, 0, s>>>(N, H, H, V.dz, g->w + P.ws(l, H), V.tmp);
@@ -452,7 +478,7 @@ gtd_status backward(gtd_gnn g, const gtd_gnn_batch* b, const Views& V, float td_
     GTD_CUDA(h, cudaGetLastError());
   }
   gtd::relu_mask<<<eb, 256, 0, s>>>(NH, V.Z, V.dh, V.dz);
-  gtd::weight_grad<<<cb, 256, 0, s>>>(N, g->fin, H, V.x, V.dz, gr + P.w_in, gr + P.b_in);
+  wgrad(s, N, g->fin, H, V.x, V.dz, gr + P.w_in, gr + P.b_in, V.part);
   GTD_CUDA(h, cudaGetLastError());
   return GTD_OK;
 }

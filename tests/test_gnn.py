@@ -87,6 +87,23 @@ def test_gpu_forward_and_gradients_match_reference(handle):
 
 
 @pytest.mark.gpu
+def test_training_is_deterministic(handle):
+    """Weight gradients are summed in a fixed order (no float atomics), so
+    the same seed and batches give bit-identical parameters."""
+    gs, b = _toy_batch(4)
+    big = gnn.make_batch(G.config3_graphs(count=300, seed=4))  # > 64 nodes: several gradient chunks
+    big.root_label = (np.arange(len(big.x)) % 3 == 0).astype(np.float32)
+    big.node_mask = np.ones(len(big.x), dtype=np.float32)
+    big.td_label = np.full(len(big.graph_start) - 1, 5.0, dtype=np.float32)
+    nets = [gnn.GNN(handle, seed=11) for _ in range(2)]
+    for net in nets:
+        for _ in range(3):
+            net.train_step(b)
+            net.train_step(big)
+    assert np.array_equal(nets[0].params(), nets[1].params())
+
+
+@pytest.mark.gpu
 def test_label_set_matches_oracle(handle, port):
     base = G.config3_graphs(count=6, seed=23)
     data = gnn.label_set(handle, base, per_graph=12, seed=3)
