@@ -61,6 +61,7 @@ def parse_args():
     ap.add_argument("--tile-bits", type=int, default=0,
                     help="DP tile bits (0 = the library's default)")
     ap.add_argument("--no-c3", action="store_true", help="skip the batched DP measurement")
+    ap.add_argument("--c3-graphs", type=int, default=4096, help="graphs of the batched DP measurement (config 3)")
     ap.add_argument("--no-bnb", action="store_true", help="skip the plain vs learned B&B measurement")
     ap.add_argument("--bnb-graphs", type=int, default=None,
                     help="B&B graphs (default 256 of config 4; 1024 of config 5 with --workload bnb-c5)")
@@ -255,13 +256,13 @@ def run_reference(args, graphs):
 # GPU arm.
 # ---------------------------------------------------------------------------
 
-def measure_dp_c3(h, steps, warmup):
+def measure_dp_c3(h, steps, warmup, count=4096):
     """Batched uneven DP on config 3 (4096 graphs), device time from the
     library's events and host time of the whole C-ABI call."""
     from gisbdw_gb300 import _lib
     from gisbdw_gb300 import graphs as G
     from gisbdw_gb300.validate import check_tree
-    graphs = G.config3_graphs()
+    graphs = G.config3_graphs(count=count)
     packed = _lib.pack_batch(graphs)
     t0 = time.perf_counter()
     rates = h.dp_autotune(10, 24)  # subsets/us per (n, tile bits 8..12); the planner picks from these
@@ -481,7 +482,7 @@ def run_gpu(args, graphs):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_c3:
-        line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup)
+        line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup, args.c3_graphs)
     if rank == 0 and not args.no_bnb:
         line["bnb_c4"] = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
                                      0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes)
