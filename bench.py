@@ -292,7 +292,7 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     stream; identical graphs in both arms), the GNN trained here on DP
     labels."""
     import numpy as np
-    from gisbdw_gb300 import gnn
+    from gisbdw_gb300 import _lib, gnn
     from gisbdw_gb300 import graphs as G
     from gisbdw_gb300.validate import check_tree
     base = gnn.training_graphs(n_label, seed=11)
@@ -307,7 +307,10 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     graphs = G.config4_graphs(count=n_graphs) if family == "c4" else G.config5_graphs(count=n_graphs)
     cap_ns = int(cap_s * 1e9)
     h.bnb_solve_batch(graphs[:4], deadline_ns=10**8, memo_log2=memo_log2)  # warm-up (allocation, module load)
-    plain = h.bnb_solve_batch(graphs, deadline_ns=cap_ns, memo_log2=memo_log2)
+    tp = time.perf_counter()
+    packed = _lib.pack_bnb(graphs)  # the reference heuristic's incumbents (host), counted in e2e
+    t_seed = time.perf_counter() - tp
+    plain = h.bnb_solve_batch(graphs, deadline_ns=cap_ns, memo_log2=memo_log2, packed=packed)
     t3 = time.perf_counter()
     gd = gnn.guidance(net, graphs)
     t_inf = time.perf_counter() - t3
@@ -331,7 +334,7 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
                 "p50_nodes_per_proven_graph": float(np.median(res["nodes"][ok])) if ok.any() else None,
                 "trees_valid": all(check_tree(g, int(t), par) for g, t, par in
                                    zip(graphs, res["td"], res["parents"]))}
-    ps, ls = summary(plain), summary(learned, t_inf)
+    ps, ls = summary(plain, t_seed), summary(learned, t_inf)
     solved = learned["status"] == 0
     ls["td_estimate_mae_on_proven"] = float(np.abs(gd["td_est"][solved] - learned["td"][solved]).mean()) \
         if solved.any() else None
@@ -339,7 +342,8 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     out = {"graphs": len(graphs), "cap_s": cap_s, "plain": ps, "learned": ls, "both_solved": int(both.sum()),
            "td_identical_on_both": bool(np.array_equal(plain["td"][both], learned["td"][both])),
            "gnn": {"labels": len(samples), "label_s": t1 - t0, "train_s": t2 - t1, "train_steps": len(losses),
-                   "held_out": acc, "inference_s": t_inf, "layers": gnn.LAYERS, "hidden": gnn.HIDDEN,
+                   "held_out": acc, "inference_s": t_inf, "plain_seed_s": t_seed,
+                   "layers": gnn.LAYERS, "hidden": gnn.HIDDEN,
                    "weights": "bf16 (fp32 master, fp32 accumulation)"}}
     if both.any():
         pp, lp = np.median(plain["proof_ms"][both]), np.median(learned["proof_ms"][both])
