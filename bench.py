@@ -308,7 +308,8 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     cap_ns = int(cap_s * 1e9)
     h.bnb_solve_batch(graphs[:4], deadline_ns=10**8, memo_log2=memo_log2)  # warm-up (allocation, module load)
     tp = time.perf_counter()
-    packed = _lib.pack_bnb(graphs)  # the reference heuristic's incumbents (host), counted in e2e
+    std, spar = h.heuristic_batch(graphs, 0)  # the reference heuristic chain's incumbents, counted in e2e
+    packed = _lib.pack_bnb(graphs, seeds=list(zip(std.tolist(), spar)))
     t_seed = time.perf_counter() - tp
     plain = h.bnb_solve_batch(graphs, deadline_ns=cap_ns, memo_log2=memo_log2, packed=packed)
     t3 = time.perf_counter()

@@ -295,6 +295,29 @@ def _bind_bnb(L):
     return L
 
 
+def _heuristic_batch(self, graphs, kind: int = 0, scores=None):
+    """gtd_heuristic on the GPU for every graph (gtd_heuristic_batch):
+    returns (td[count], [parent arrays])."""
+    L = _bind_bnb(self.L)
+    if not getattr(L, "_hb_bound", False):
+        L.gtd_heuristic_batch.argtypes = [_vp, _vp, _i, _vp, ctypes.c_int64, _i, _vp, _vp, _vp]
+        L._hb_bound = True
+    ns = np.array([g.n for g in graphs], dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32)
+    descs = np.ascontiguousarray(np.stack([ns, offs], axis=1))
+    adj = np.ascontiguousarray(np.concatenate([g.adj128() for g in graphs]).astype(np.uint64))
+    total = int(ns.sum())
+    sc = np.ascontiguousarray(np.concatenate(scores), dtype=np.float32) if scores is not None else None
+    td = np.zeros(len(graphs), dtype=np.int32)
+    par = np.zeros(total, dtype=np.int32)
+    self._check(L.gtd_heuristic_batch(self._h, _ptr(descs), len(graphs), _ptr(adj), total, kind,
+                                      _ptr(sc) if sc is not None else None, _ptr(td), _ptr(par)))
+    return td, [par[o:o + n].copy() for o, n in zip(offs, ns)]
+
+
+Handle.heuristic_batch = _heuristic_batch
+
+
 def heuristic(g, kind: int = 0, scores=None):
     """Greedy incumbent (gtd_heuristic): kind 0 HighestDegree(Variance),
     1 HighestDegree, 2 Variance, 3 highest score first. Host only."""
@@ -338,6 +361,10 @@ def _bnb_method(self, graphs, orders=None, seeds=None, memo_log2: int = 0, deadl
     """Exact treedepth of every graph by the persistent B&B kernel.
     Returns dict: td, parents, status, proof_ms, nodes, stats."""
     L = _bind_bnb(self.L)
+    if packed is None and seeds is None:
+        # the reference heuristic chain's incumbents, all graphs in one GPU launch
+        std, spar = self.heuristic_batch(graphs, 0)
+        seeds = list(zip(std.tolist(), spar))
     descs, adj, order, seed_td, seed_par, total = packed if packed is not None else pack_bnb(graphs, orders, seeds)
     count = len(descs)
     td = np.zeros(count, dtype=np.int32)

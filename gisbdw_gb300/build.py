@@ -20,7 +20,7 @@ LIB = os.path.join(OUT_DIR, "libgtd.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC] + ARCH
 
 

@@ -473,14 +473,12 @@ def guidance(net: GNN, graphs: Sequence[Graph]) -> dict:
     first). None of it prunes."""
     b = make_batch(graphs)
     logits, td_est = net.forward(b)
-    orders, seeds = [], []
-    for k, g in enumerate(graphs):
-        s, e = b.graph_start[k], b.graph_start[k + 1]
-        sc = logits[s:e]
-        orders.append(np.argsort(-sc, kind="stable").astype(np.uint8))
-        t0, p0 = _lib.heuristic(g, 0)
-        t1, p1 = _lib.heuristic(g, 3, sc)
-        seeds.append((t1, p1) if t1 < t0 else (t0, p0))
+    scores = [logits[b.graph_start[k]:b.graph_start[k + 1]] for k in range(len(graphs))]
+    orders = [np.argsort(-sc, kind="stable").astype(np.uint8) for sc in scores]
+    # both incumbents of every graph in two GPU launches (gtd_heuristic_batch)
+    t0, p0 = net.h.heuristic_batch(graphs, 0)
+    t1, p1 = net.h.heuristic_batch(graphs, 3, scores)
+    seeds = [(int(t1[k]), p1[k]) if t1[k] < t0[k] else (int(t0[k]), p0[k]) for k in range(len(graphs))]
     hints = np.clip(np.rint(td_est), 1, None).astype(np.int32)
     return {"orders": orders, "seeds": seeds, "hints": hints, "td_est": td_est}
 

@@ -227,6 +227,18 @@ gtd_status gtd_heuristic(const uint64_t* adj2, int n, int kind,
                          const float* scores, int32_t* td_out,
                          int32_t* parent_out);
 
+/* The same heuristics for many graphs in one GPU launch (one warp per
+ * graph, n <= 128), trees identical to gtd_heuristic's: descs and the
+ * (lo, hi) adjacency pool as for gtd_bnb_solve_batch; kind 0..3 as above
+ * (kind 3 reads scores_pool[descs[i].offset + v]); td_out[count] and
+ * parent_out[pool_len] (graph i's tree at descs[i].offset). Disconnected
+ * graphs give an elimination forest. Host pointers. */
+gtd_status gtd_heuristic_batch(gtd_handle h, const gtd_graph_desc* descs,
+                               int count, const uint64_t* adj2_pool,
+                               int64_t pool_len, int kind,
+                               const float* scores_pool, int32_t* td_out,
+                               int32_t* parent_out);
+
 /* Training labels from the last single-graph DP solve: for subsets[i], its
  * treedepth td_out[i] and, when the subset is connected, the mask of its
  * optimal roots roots_out[i] (v with td(S - v) = td(S) - 1, the root set every

@@ -1,7 +1,9 @@
 """Incumbent heuristics of the library (gtd_heuristic, host code) against
 the oracle's restatement of the reference heuristics and the reference's own
-outputs (golden fixtures). CPU only."""
+outputs (golden fixtures) on CPU; the batched GPU restatement against the
+host code."""
 import numpy as np
+import pytest
 
 from gisbdw_gb300 import _lib
 from gisbdw_gb300 import graphs as G
@@ -32,3 +34,20 @@ def test_score_greedy_is_valid(port):
     scores = np.random.default_rng(0).random(g.n).astype(np.float32)
     td, par = _lib.heuristic(g, 3, scores)
     assert port.check_valid(g, td, par) if g.n <= 64 else True
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
+def test_gpu_batch_heuristics_equal_host(handle, kind):
+    """gtd_heuristic_batch (one warp per graph) gives exactly the host's
+    trees: same picks, same floating-point variance scores."""
+    gs = (G.config3_graphs(count=60, seed=31) + G.config4_graphs(count=24, seed=32)
+          + [g for g in G.config5_graphs(count=24, seed=33)]
+          + [G.path(100), G.tree_plus_edges(104, 6, 2), G.Graph(9, [(0, 1), (2, 3), (3, 4)])])
+    rng = np.random.default_rng(kind)
+    scores = [rng.random(g.n).astype(np.float32) for g in gs] if kind == 3 else None
+    td, pars = handle.heuristic_batch(gs, kind, scores)
+    for i, g in enumerate(gs):
+        htd, hpar = _lib.heuristic(g, kind, scores[i] if scores is not None else None)
+        assert td[i] == htd, (g.name, kind)
+        assert pars[i].tolist() == hpar.tolist(), (g.name, kind)
