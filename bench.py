@@ -349,6 +349,18 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     if both.any():
         pp, lp = np.median(plain["proof_ms"][both]), np.median(learned["proof_ms"][both])
         out["p50_proof_ms_both"] = {"plain": float(pp), "learned": float(lp), "plain_over_learned": float(pp / lp)}
+    if family == "c5":
+        # the same stream with the small graphs (n <= 28) given to the subset DP
+        from gisbdw_gb300 import solve_exact
+        hy = solve_exact(h, graphs, dp_max_n=28, deadline_ns=cap_ns, guidance=gd, memo_log2=memo_log2)
+        ok = hy["status"] == 0
+        by_dp = np.array([s == "dp" for s in hy["solver"]])
+        agree = (learned["status"] == 0) & ok
+        out["hybrid_learned"] = {
+            "solved": int(ok.sum()), "by_dp": int(by_dp.sum()),
+            "p50_proof_ms_capped": float(np.median(np.where(ok, hy["proof_ms"], cap_s * 1e3))),
+            "td_identical_to_learned_bnb": bool(np.array_equal(hy["td"][agree], learned["td"][agree])),
+            "trees_valid": all(check_tree(g, int(t), par) for g, t, par in zip(graphs, hy["td"], hy["parents"]))}
     if cpu_sample:
         threads = os.cpu_count() or 1
         sample = graphs[:cpu_sample]

@@ -8,7 +8,7 @@ seeded graph generators and text IO (``graphs``) and the build script
 """
 from . import graphs
 from ._lib import GtdError, InvalidArgument, DeadlineExceeded, Handle
-from .treedepth import BnBGPU, DynamicGPU, Result
+from .treedepth import BnBGPU, DynamicGPU, Result, solve_exact
 
 __all__ = ["graphs", "GtdError", "InvalidArgument", "DeadlineExceeded", "Handle",
-           "DynamicGPU", "BnBGPU", "Result"]
+           "DynamicGPU", "BnBGPU", "Result", "solve_exact"]

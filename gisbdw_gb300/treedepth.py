@@ -128,3 +128,42 @@ class BnBGPU:
             raise _lib.GtdError(7, "no solve yet")
         par = self._res["parents"][0]
         return Result(int(self._res["td"][0]), int(np.flatnonzero(par == -1)[0]), par.copy())
+
+
+def solve_exact(handle: _lib.Handle, graphs, dp_max_n: int = 28, deadline_ns: int = 0, guidance=None,
+                **bnb_kw) -> dict:
+    """Exact treedepth of many connected graphs, each by the solver that suits
+    its size: graphs with n <= dp_max_n by the batched subset DP (every one
+    proven, in one launch), the others by the batched branch and bound
+    (optionally guided: `guidance` = gnn.guidance(net, graphs)).
+
+    Returns td, parents, status (0 proven, 4 deadline), proof_ms (per graph,
+    from the start of the call; DP graphs: the DP batch's device time) and
+    which solver took each graph ("dp" / "bnb")."""
+    import time
+    n_all = len(graphs)
+    small = [i for i, g in enumerate(graphs) if g.n <= dp_max_n]
+    large = [i for i, g in enumerate(graphs) if g.n > dp_max_n]
+    td = np.zeros(n_all, dtype=np.int32)
+    status = np.zeros(n_all, dtype=np.int32)
+    proof = np.zeros(n_all, dtype=np.float32)
+    parents = [None] * n_all
+    solver = [""] * n_all
+    t0 = time.perf_counter()
+    if small:
+        dtd, dpar, st = handle.dp_solve_batch([graphs[i] for i in small])
+        for j, i in enumerate(small):
+            td[i], parents[i], solver[i] = dtd[j], dpar[j], "dp"
+            proof[i] = st["total_ms"]
+    if large:
+        sub = [graphs[i] for i in large]
+        kw = dict(bnb_kw)
+        if guidance is not None:
+            kw.update(orders=[guidance["orders"][i] for i in large], seeds=[guidance["seeds"][i] for i in large],
+                      hints=np.asarray(guidance["hints"])[large])
+        off_ms = (time.perf_counter() - t0) * 1e3
+        res = handle.bnb_solve_batch(sub, deadline_ns=deadline_ns, **kw)
+        for j, i in enumerate(large):
+            td[i], parents[i], status[i], solver[i] = res["td"][j], res["parents"][j], res["status"][j], "bnb"
+            proof[i] = res["proof_ms"][j] + off_ms if res["status"][j] == 0 else -1.0
+    return {"td": td, "parents": parents, "status": status, "proof_ms": proof, "solver": solver}

@@ -132,3 +132,15 @@ def test_bnb_graphs_wider_than_64_vertices(handle):
     assert set(r2["status"].tolist()) <= {0, 4}
     for g, t, par in zip(rs, r2["td"], r2["parents"]):
         assert check_tree(g, t, par), g.name
+
+
+def test_solve_exact_dispatches_by_size(handle):
+    from gisbdw_gb300 import solve_exact
+    gs = [G.gnp_connected(18, 0.2, 3), G.grid(4, 6), G.tree_plus_edges(40, 4, 5), G.cycle(33)]
+    res = solve_exact(handle, gs, dp_max_n=24, deadline_ns=CAP_NS)
+    assert res["solver"] == ["dp", "dp", "bnb", "bnb"]
+    assert np.all(res["status"] == 0)
+    for g, t, par in zip(gs, res["td"], res["parents"]):
+        assert check_tree(g, int(t), par), g.name
+    assert res["td"][0] == handle.dp_solve(gs[0].adj64(), gs[0].n)[0]
+    assert res["td"][3] == 1 + 6  # cycle: 1 + ceil(log2(33))
