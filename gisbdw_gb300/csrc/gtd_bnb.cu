@@ -356,12 +356,15 @@ struct Search {
     return __popcll(w->alo[v] & lo) + __popcll(w->ahi[v] & hi);
   }
 
-  // Longest-path bound: td(C) >= ceil(log2(L + 1)) for a path of L vertices
-  // in C (treedepth is monotone under subgraphs and td(P_L) = ceil(log2(L +
-  // 1))). Each lane grows one path greedily from its own start vertex,
-  // extending one end by the neighbour with the fewest unvisited neighbours
-  // (Warnsdorff's rule) until it is stuck, then the other end, and stops
-  // once the path has `need` vertices. The bound is the longest over lanes.
+  // Path and cycle bound: td(C) >= ceil(log2(L + 1)) for a path of L
+  // vertices in C, and td(C) >= 1 + ceil(log2(m)) for a cycle of m >= 3
+  // vertices (treedepth is monotone under subgraphs; td(P_L) =
+  // ceil(log2(L + 1)), and C_m minus any vertex is P_(m-1)). Each lane grows
+  // one path greedily from its own start vertex, extending one end by the
+  // neighbour with the fewest unvisited neighbours (Warnsdorff's rule) until
+  // it is stuck, then the other end, and stops once the path has `need`
+  // vertices; every chord between path vertices i < j positions apart
+  // closes a cycle of j - i + 1 vertices. The bound is the best over lanes.
   __device__ int path_lb(uint64_t Clo, uint64_t Chi, int need) const {
     int start = -1;
 #pragma unroll
@@ -370,11 +373,13 @@ struct Search {
       if (start < 0 && u < n && has(Clo, Chi, u))
         start = u;
     }
-    uint32_t len = 0;
+    uint32_t len = 0, cyc = 0;
     if (start >= 0) {
+      int8_t pos[kBnbMaxN];  // position on the path: front >= 0, back < 0
       uint64_t plo = 0, phi = 0;
       bit_set(plo, phi, start);
-      int e0 = start, e1 = start, side = 0, stuck = 0;
+      pos[start] = 0;
+      int e0 = start, e1 = start, side = 0, stuck = 0, front = 0, back = 0;
       len = 1;
       while (static_cast<int>(len) < need && stuck < 2) {
         const int e = side ? e1 : e0;
@@ -395,15 +400,34 @@ struct Search {
           }
         }
         bit_set(plo, phi, best);
-        if (side)
+        if (side) {
           e1 = best;
-        else
+          pos[best] = static_cast<int8_t>(-(++back));
+        } else {
           e0 = best;
+          pos[best] = static_cast<int8_t>(++front);
+        }
         ++len;
       }
+      // the path alone does not refute; a cycle on it can (it has at most len
+      // vertices and needs more than need / 2)
+      if (static_cast<int>(len) < need && static_cast<int>(len) > (need >> 1)) {
+        for (uint64_t xlo = plo, xhi = phi; xlo | xhi;) {
+          const int v = first128(xlo, xhi);
+          bit_clear(xlo, xhi, v);
+          for (uint64_t ylo = w->alo[v] & plo, yhi = w->ahi[v] & phi; ylo | yhi;) {
+            const int u = first128(ylo, yhi);
+            bit_clear(ylo, yhi, u);
+            const int d = pos[u] - pos[v];
+            if (d >= 2)
+              cyc = max(cyc, static_cast<uint32_t>(d + 1));
+          }
+        }
+      }
     }
-    len = __reduce_max_sync(0xffffffffu, len);
-    return 32 - __clz(static_cast<int>(len));
+    const int lb_path = 32 - __clz(static_cast<int>(len));
+    const int lb_cyc = cyc >= 3 ? 1 + (32 - __clz(static_cast<int>(cyc - 1))) : 0;
+    return static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<uint32_t>(max(lb_path, lb_cyc))));
   }
 
   // Memo bounds of the vertex-deleted subsets C - v (one lookup per vertex,
@@ -674,14 +698,17 @@ struct Search {
             } else if (hit.lb > fk) {
               verdict = 0;
             } else {
-              int lb = max(hit.lb, edge_lb(csize, edges(f.lo, f.hi)));
+              const int ecount = edges(f.lo, f.hi);
+              int lb = max(hit.lb, edge_lb(csize, ecount));
               if (lb <= fk && hit.lb == 0 && csize >= kMmdMin) {
                 lb = max(lb, mmd_lb(f.lo, f.hi));
                 if (lane == 0)
                   memo_put(memo, memo_mask, f.lo, f.hi, lb, kUnknownUb, 0);
               }
-              // a path of 2^fk vertices would refute td <= fk
-              if (lb <= fk && fk < 7 && (1 << fk) <= csize) {
+              // a path of 2^fk vertices, or a cycle of 2^(fk-1) + 1, would
+              // refute td <= fk (a tree, with fewer edges than vertices, has
+              // no cycle)
+              if (lb <= fk && fk < 8 && ((1 << fk) <= csize || (ecount >= csize && (1 << (fk - 1)) < csize))) {
                 const int pl = path_lb(f.lo, f.hi, 1 << fk);
                 if (pl > fk) {
                   lb = pl;
