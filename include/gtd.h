@@ -178,7 +178,8 @@ gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max,
 #define GTD_BNB_MAX_N 104
 
 typedef struct {
-  int memo_log2;        /* memo slots per graph = 2^memo_log2 (0 = sized from free HBM, 2^16..2^24) */
+  int memo_log2;        /* memo slots per graph = 2^memo_log2 (0 = sized from free HBM: a quarter,
+                           at most 32 GiB, 2^16..2^24 slots of 16 bytes) */
   uint64_t deadline_ns; /* per-graph cap on time-to-proof (0 = 120 s) */
   int ctas_per_sm;      /* 0 = occupancy limit */
   const int32_t* level_hint; /* per graph, NULL or 0 = none: the decision level
@@ -195,8 +196,10 @@ typedef struct {
 } gtd_bnb_stats;
 
 /* BranchAndBound (Treedepth/src/branch_and_bound/branch_and_bound.cpp:51-114)
- * and BnBGPU (bnb_gpu.cu:264-380) over a batch of connected graphs in one
- * persistent launch: exact treedepth AND an elimination tree per graph (the
+ * and BnBGPU (bnb_gpu.cu:264-380) over a batch of connected graphs in
+ * persistent launches (passes of node-budgeted items; a batch too small to
+ * fill the GPU is split into first-root x second-root items, so a single
+ * graph uses n^2 warps): exact treedepth AND an elimination tree per graph (the
  * reference's GPU B&B returns the treedepth only). Graph i has n = descs[i].n
  * <= GTD_BNB_MAX_N vertices with 128-bit adjacency masks
  * adj2_pool[2 (offset + v)] (bits 0-63) and [2 (offset + v) + 1] (bits
