@@ -144,3 +144,18 @@ def test_solve_exact_dispatches_by_size(handle):
         assert check_tree(g, int(t), par), g.name
     assert res["td"][0] == handle.dp_solve(gs[0].adj64(), gs[0].n)[0]
     assert res["td"][3] == 1 + 6  # cycle: 1 + ceil(log2(33))
+
+
+def test_smallest_graphs_every_solver(handle):
+    """n = 1 and n = 2 (and a clique, td = n) through the DP, the B&B and
+    the batched heuristics."""
+    gs = [G.Graph(1, []), G.path(2), G.complete(5), G.path(3)]
+    want = [1, 2, 5, 2]
+    res = _check(handle, gs)
+    assert res["td"].tolist() == want
+    for g, t in zip(gs, want):
+        assert handle.dp_solve(g.adj64(), g.n)[0] == t
+    htd, hpar = handle.heuristic_batch(gs, 0)
+    assert htd.tolist() == want  # greedy is optimal on these
+    for g, t, par in zip(gs, htd, hpar):
+        assert check_tree(g, int(t), par)
