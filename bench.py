@@ -43,6 +43,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "exact-treedepth solves/s & p50 time-to-proof: learned-guided vs plain GPU B&B"
+WORKLOAD_C2 = ("dp-c2 (config 2: 8 connected G(n,p), n in {28,30,32}, p in {0.1,0.2,0.3}, seeds 1-8, "
+               "+ grid 5x6; exact DP + elimination tree per graph)")
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
@@ -243,8 +245,8 @@ def run_reference(args, graphs):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / len(times), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "dp-c2 (config 2: 8 G(n,p) n in {28,30,32} + grid 5x6)",
-                   "sample": "n=28 graphs only"},
+        "config": {"workload": WORKLOAD_C2, "l2": "working set (DP tables 256 MiB-4 GiB) > L2",
+                   "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
                          "sample": desc, "cpu": cpu_model()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -480,8 +482,7 @@ def run_gpu(args, graphs):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic",
-        "config": {"workload": "dp-c2 (config 2: 8 connected G(n,p), n in {28,30,32}, p in {0.1,0.2,0.3}, "
-                               "seeds 1-8, + grid 5x6; exact DP + elimination tree per graph)",
+        "config": {"workload": WORKLOAD_C2,
                    "graphs": [g.name for g in graphs], "l2": "working set (DP tables 256 MiB-4 GiB) > L2",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "p50_time_to_proof_ms": statistics.median(per_graph_ms),
