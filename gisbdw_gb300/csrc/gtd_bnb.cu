@@ -73,7 +73,8 @@ constexpr int kBnbWarps = 4;
 constexpr int kMaxComps = 40;            // components with >= 3 vertices: <= 104 / 3
 constexpr int kMemoProbes = 8;
 constexpr int kMmdMin = 10;              // minor-min-width bound for |C| >= this
-constexpr int kSubsetMin = 16;           // memo bounds of the C - v for |C| >= this
+constexpr int kSubsetMin = 16;
+constexpr int kMiniMin = 6, kMiniMax = 10;  // components decided exactly by a subset DP           // memo bounds of the C - v for |C| >= this
 constexpr uint32_t kSeedRoot = 0xFFu;
 constexpr int kUnknownUb = 127;
 constexpr int kIoUnfinished = 3;         // d_io word: items that spent their budget this round
@@ -114,6 +115,7 @@ struct BnbParams {
   int window = 0;                  // levels run at a time below a graph's top level (0 = all)
   int split = 0;                   // 1: an item is a pair (first root, second root)
   uint32_t* unfinished = nullptr;  // items that used up their budget this round
+  uint8_t* mini = nullptr;         // per warp: 2^kMiniMax-byte small-component DP table
   uint32_t* exited = nullptr;      // [0] warps that found no ticket left, [1] items started (this pass)
   uint32_t drain_at = 0;           // running items yield once this many warps have left
   uint32_t full_at = 0;            // ... and at least this many items have started
@@ -148,6 +150,8 @@ struct WarpMem {
   uint8_t qown[kBnbMaxN], qk[kBnbMaxN], qdep[kBnbMaxN];
   uint8_t ssz[kMaxComps];
   uint8_t order[kBnbMaxN];
+  uint8_t mvert[kMiniMax];   // small-component DP: vertex of each local id
+  uint16_t madj[kMiniMax];   // ... and its local adjacency
 };
 
 __device__ __forceinline__ bool has(uint64_t lo, uint64_t hi, int v) {
@@ -303,6 +307,67 @@ struct Search {
   unsigned long long nodes;
   bool timed_out, cancelled;
   bool yielded = false;
+  uint8_t* mini = nullptr;  // this warp's 2^kMiniMax-byte table in global memory (L1-resident)
+
+  // Exact treedepth of a component of m <= kMiniMax vertices by the subset
+  // DP of the single-graph kernel (the reference's TreedepthInfo bound,
+  // branch_and_bound.hpp:27-28, computed rather than looked up): byte of S =
+  // td << 1 | connected; |S| >= 3 is connected iff two children S - v are;
+  // td = 1 + min over children if connected, else the max. Subsets are
+  // resolved level by level, lanes across each level. *root_out = the first
+  // local vertex v with td(C - v) = td(C) - 1, as a global vertex.
+  __device__ int mini_dp(uint64_t Clo, uint64_t Chi, int m, int* root_out) {
+    if (lane == 0) {
+      int i = 0;
+      for (uint64_t xlo = Clo, xhi = Chi; xlo | xhi; ++i) {
+        const int v = first128(xlo, xhi);
+        bit_clear(xlo, xhi, v);
+        w->mvert[i] = static_cast<uint8_t>(v);
+      }
+    }
+    __syncwarp();
+    if (lane < m) {
+      const int v = w->mvert[lane];
+      uint16_t a = 0;
+      for (int j = 0; j < m; ++j)
+        if (has(w->alo[v], w->ahi[v], w->mvert[j]))
+          a |= static_cast<uint16_t>(1u << j);
+      w->madj[lane] = a;
+    }
+    __syncwarp();
+    uint8_t* T = mini;
+    const uint32_t full = (1u << m) - 1u;
+    for (int l = 1; l <= m; ++l) {
+      for (uint32_t S = lane; S <= full; S += 32) {
+        if (__popc(S) != l)
+          continue;
+        uint32_t b;
+        if (l == 1) {
+          b = 3u;  // td 1, connected
+        } else if (l == 2) {
+          const int u = __ffs(S) - 1, v = 31 - __clz(S);
+          b = ((w->madj[u] >> v) & 1u) ? 5u : 2u;  // td 2 connected, or td 1 disconnected
+        } else {
+          uint32_t mn = 255u, mx = 0u, cnt = 0u;
+          for (uint32_t x = S; x; x &= x - 1) {
+            const uint32_t c = T[S & ~(x & (0u - x))];
+            mn = min(mn, c);
+            mx = max(mx, c);
+            cnt += c & 1u;
+          }
+          b = cnt >= 2u ? ((mn & ~1u) + 3u) : (mx & ~1u);
+        }
+        T[S] = static_cast<uint8_t>(b);
+      }
+      __syncwarp();
+    }
+    const int td = T[full] >> 1;
+    const bool is_root = lane < m && (T[full & ~(1u << lane)] >> 1) == static_cast<uint32_t>(td - 1);
+    const uint32_t roots = __ballot_sync(0xffffffffu, is_root);
+    *root_out = roots ? w->mvert[__ffs(roots) - 1] : w->mvert[0];
+    __syncwarp();
+    return td;
+  }
 
   __device__ void component(uint64_t Slo, uint64_t Shi, int v, uint64_t& rlo, uint64_t& rhi) const {
     rlo = v < 64 ? (1ull << v) : 0ull;
@@ -697,6 +762,13 @@ struct Search {
               vroot = hit.root;
             } else if (hit.lb > fk) {
               verdict = 0;
+            } else if (mini && csize >= kMiniMin && csize <= kMiniMax) {
+              int r = 0;
+              const int td = mini_dp(f.lo, f.hi, csize, &r);
+              if (lane == 0)
+                memo_put(memo, memo_mask, f.lo, f.hi, td, td, r);
+              verdict = td <= fk ? 1 : 0;
+              vroot = r;
             } else {
               const int ecount = edges(f.lo, f.hi);
               int lb = max(hit.lb, edge_lb(csize, ecount));
@@ -995,6 +1067,7 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 6) bnb_kernel(const __grid_con
     uint64_t fl, fh;
     full_set(G.n, fl, fh);
     Search s{w, lane, G.n, p.memo + G.memo_off, p.memo_mask, StopCheck{}, 0ull, false, false};
+    s.mini = p.mini ? p.mini + (size_t(blockIdx.x) * kBnbWarps + warp) * (1u << kMiniMax) : nullptr;
     s.stop.best = p.best + g;
     s.stop.lbp = p.lbp + g;
     s.stop.item_k = k;
@@ -1230,6 +1303,8 @@ struct gtd_bnb_state {
   size_t u64_cap = 0;
   int8_t* i8 = nullptr;    // per-level trees
   size_t i8_cap = 0;
+  uint8_t* mini = nullptr; // per-warp small-component DP tables
+  size_t mini_cap = 0;
 };
 
 void gtd_bnb_release(gtd_handle h) {
@@ -1244,6 +1319,7 @@ void gtd_bnb_release(gtd_handle h) {
   cudaFree(b->u32);
   cudaFree(b->u64);
   cudaFree(b->i8);
+  cudaFree(b->mini);
   delete b;
   h->bnb = nullptr;
 }
@@ -1415,6 +1491,8 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   const long long ctas =
       std::max(1ll, std::min<long long>(static_cast<long long>(h->num_sms) * occ, (items + kBnbWarps - 1) / kBnbWarps));
   p.drain_at = static_cast<uint32_t>(std::max(1ll, ctas * kBnbWarps / 2));
+  if ((s = grow(h, &B.mini, &B.mini_cap, size_t(ctas) * kBnbWarps * (size_t(1) << kMiniMax))) != GTD_OK) return s;
+  p.mini = B.mini;
   p.full_at = static_cast<uint32_t>(ctas * kBnbWarps);
   GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
   // Rounds: every item may spend `budget` nodes per launch; the host stops
