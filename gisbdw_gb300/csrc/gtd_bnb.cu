@@ -27,7 +27,11 @@
 //    and smaller id: v is at least as good), and a per-graph memo in HBM of
 //    a lower and an upper bound (with a root achieving it) per component,
 //    keyed by the component's vertex mask in 128-bit slots updated by
-//    atomic CAS and shared by every warp working on that graph.
+//    atomic CAS and shared by every warp working on that graph. Components
+//    of 6-10 vertices are decided exactly by the subset-DP recurrence in a
+//    per-warp table (their exact td goes to the memo); the memo bounds of
+//    the vertex-deleted subsets C - v refute (td(C) >= td(C - v)) or accept
+//    (root v) a component before any root is tried.
 //  * Schedule: persistent launches over a global atomic queue of items
 //    (graph, level k, root candidate), issued for k descending from the
 //    incumbent minus one, candidates in priority order, graphs interleaved.
