@@ -17,6 +17,14 @@
 //                                   dynamic_gpu.cu:90-111)
 //    with each table byte holding td << 1 | connected. No per-subset BFS, no
 //    ranking per child.
+//  * Reduction. Deleting a vertex lowers treedepth by at most one, so the
+//    children's treedepths are td(S) - 1 or td(S): two consecutive values at
+//    most. Their OR plus their AND is then 2a + 1 when both a and a + 1
+//    occur (td(S) = a + 1, connected or not) and 2v when all equal v
+//    (td(S) = v + connected(S)), so with s = OR + AND,
+//      td(S) = (s >> 1) + ((s & 1) | connected(S)).
+//    OR and AND of the raw bytes are plain 32-bit logic over 4 subsets at
+//    once; a third word collects "at least two connected children" in bit 0.
 //  * Layout (gtd_dp_layout.h). Tiles of 2^lb subsets share a high part H;
 //    a tile's cross-tile children are the whole tiles H - h one level down,
 //    read as contiguous 2^lb-byte blocks (16-byte vector loads through L2);
@@ -26,11 +34,8 @@
 //    worker (no CTA barriers in the loop). A warp takes a tile by ticket
 //    (atomicAdd) in level-major order, its lanes wait on the ready flags of
 //    the |H| child tiles (each wait bounded by a deadline), the warp reduces
-//    the children with 2 x 16-bit DPX min/max (__vimin3_u16x2 /
-//    __vimax3_u16x2, three operands per instruction, after unpacking each
-//    byte word into two 16-bit pair words; byte-lane SIMD min/max has no
-//    native instruction here), resolves the tile, stores it and publishes
-//    its flag. A tile only waits on tiles with smaller tickets,
+//    the children with OR / AND / majority logic on 4-byte words, resolves
+//    the tile, stores it and publishes its flag. A tile only waits on tiles with smaller tickets,
 //    and a ticket is only taken by a running warp, so the smallest unfinished
 //    ticket can always proceed.
 //
@@ -55,7 +60,7 @@ struct TileShape {
   static constexpr int kEntries = 1 << LB;
   static constexpr int kWords = kEntries / 4;   // 4 subsets per 32-bit word
   static constexpr int kWordBits = LB - 2;
-  // dynamic shared memory: per warp T, MN, MX, CT (kWords words each), then
+  // dynamic shared memory: per warp T, OR, AND, CT (kWords words each), then
   // the shared word order (kWords uint16).
   static constexpr size_t kPerWarp = size_t(4) * kWords * 4;
   static constexpr size_t kOrderOff = size_t(kDpWarps) * kPerWarp;
@@ -64,59 +69,52 @@ struct TileShape {
 
 using Binom = uint32_t[kDpMaxHigh + 1][kDpMaxHigh + 1];
 
-// Table bytes hold td << 1 | connected, so an unsigned min (max) over
-// children gives 2 * min td (2 * max td) plus a flag bit, without masking.
-// Byte-wise SIMD (__vminu4) is emulated on this GPU, so words are split into
-// two 16x2 halves (bytes 0,2 and bytes 1,3) and reduced with the 16-bit
-// two-lane min/max, which are native.
-__device__ __forceinline__ uint32_t lo16(uint32_t x) { return __byte_perm(x, 0u, 0x4240u); }
-__device__ __forceinline__ uint32_t hi16(uint32_t x) { return __byte_perm(x, 0u, 0x4341u); }
-// bytes (l.lane0, h.lane0, l.lane1, h.lane1) back into one word
-__device__ __forceinline__ uint32_t pack16(uint32_t l, uint32_t h) { return __byte_perm(l, h, 0x6240u); }
-
-struct Agg {
-  uint32_t mnl, mnh, mxl, mxh, ct;  // min/max of bytes (0,2) and (1,3); connected-child counts (bytes)
+// Per word (4 subsets, one per byte): o = OR and a = AND of the children's
+// bytes, d = "at least two connected children" in bit 0 of each byte.
+struct Acc {
+  uint32_t o, a, d;
 };
 
-__device__ __forceinline__ void agg_init(Agg& a) {
-  a.mnl = a.mnh = 0xFFFFFFFFu;
-  a.mxl = a.mxh = 0u;
-  a.ct = 0u;
+__device__ __forceinline__ void acc_init(Acc& c) {
+  c.o = 0u;
+  c.a = 0xFFFFFFFFu;
+  c.d = 0u;
 }
 
-__device__ __forceinline__ void agg_add2(Agg& a, uint32_t x, uint32_t y) {
-  const uint32_t xl = lo16(x), xh = hi16(x), yl = lo16(y), yh = hi16(y);
-  a.mnl = __vimin3_u16x2(a.mnl, xl, yl);
-  a.mnh = __vimin3_u16x2(a.mnh, xh, yh);
-  a.mxl = __vimax3_u16x2(a.mxl, xl, yl);
-  a.mxh = __vimax3_u16x2(a.mxh, xh, yh);
-  a.ct += (x & 0x01010101u) + (y & 0x01010101u);
+__device__ __forceinline__ void acc_add2(Acc& c, uint32_t x, uint32_t y) {
+  c.d |= (c.o & (x | y)) | (x & y);  // majority of (any before, x, y)
+  c.o |= x | y;
+  c.a &= x & y;
 }
 
-__device__ __forceinline__ void agg_add1(Agg& a, uint32_t x) {
-  const uint32_t xl = lo16(x), xh = hi16(x);
-  a.mnl = __vminu2(a.mnl, xl);
-  a.mnh = __vminu2(a.mnh, xh);
-  a.mxl = __vmaxu2(a.mxl, xl);
-  a.mxh = __vmaxu2(a.mxh, xh);
-  a.ct += x & 0x01010101u;
+__device__ __forceinline__ void acc_add1(Acc& c, uint32_t x) {
+  c.d |= c.o & x;
+  c.o |= x;
+  c.a &= x;
 }
 
-// Scalar value of one subset from the min/max raw child bytes m, M, the
-// number c of connected children and k = |S|; `adjacent` is used when k == 2.
-__device__ __forceinline__ uint32_t resolve(uint32_t m, uint32_t M, uint32_t c, int k, bool adjacent) {
-  if (k <= 1)
-    return k == 0 ? 0u : 3u;  // empty set: td 0; singleton: td 1, connected
-  const bool conn = k == 2 ? adjacent : c >= 2u;  // >= 2 non-cut vertices <=> connected
-  return conn ? ((m & ~1u) + 3u) : (M & ~1u);
+// Four subsets with |S| >= 3 (connected <=> >= 2 connected children) and at
+// least one child each: per byte s = OR(td) + AND(td) <= 126, so no carries.
+__device__ __forceinline__ uint32_t resolve4(const Acc& c) {
+  const uint32_t s = ((c.o & 0xFEFEFEFEu) + (c.a & 0xFEFEFEFEu)) >> 1;
+  const uint32_t cn = c.d & 0x01010101u;
+  return ((s & 0xFEFEFEFEu) + (((s | cn) & 0x01010101u) << 1)) | cn;
 }
 
-// Two subsets at once (16-bit lanes, values in the low byte), |S| >= 3:
-// connected (>= 2 connected children) -> 2 (min td + 1) + 1, else 2 max td.
-__device__ __forceinline__ uint32_t resolve2(uint32_t mn, uint32_t mx, uint32_t ct) {
-  const uint32_t h = (ct + 0x7FFE7FFEu) & 0x80008000u;  // bit 15: count >= 2
-  const uint32_t m = h - (h >> 15);
-  return (((mn & 0xFFFEFFFEu) + 0x00030003u) & m) | (mx & 0xFFFEFFFEu & ~m);
+// One subset of size k from its children's OR o, AND a and count flag d;
+// `adjacent` gives connectivity when k == 2.
+__device__ __forceinline__ uint32_t resolve1(uint32_t o, uint32_t a, uint32_t d, int k, bool adjacent) {
+  if (k == 0)
+    return 0u;  // empty set: td 0
+  const uint32_t cn = k == 1 ? 1u : k == 2 ? (adjacent ? 1u : 0u) : (d & 1u);
+  const uint32_t s = ((o & 0xFEu) + (a & 0xFEu)) >> 1;
+  return ((s & 0xFEu) + (((s | cn) & 1u) << 1)) | cn;
+}
+
+__device__ __forceinline__ void fold1(uint32_t& o, uint32_t& a, uint32_t& d, uint32_t v) {
+  d |= o & v;
+  o |= v;
+  a &= v;
 }
 
 // Level j, high part H and level offsets of local tile t of a graph with nh
@@ -209,9 +207,9 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   uint32_t* T = reinterpret_cast<uint32_t*>(smem + size_t(warp) * Shape::kPerWarp);
-  uint32_t* MN = T + kWords;
-  uint32_t* MX = MN + kWords;
-  uint32_t* CT = MX + kWords;
+  uint32_t* OR = T + kWords;
+  uint32_t* AND = OR + kWords;
+  uint32_t* CT = AND + kWords;
   uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + Shape::kOrderOff);
   const Binom& binom = p.binom;
 
@@ -265,52 +263,48 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       break;
 
     // Cross-tile children: j whole tiles, 4 subsets per word, children two
-    // at a time through the 3-way 16-bit min/max.
+    // at a time.
     if constexpr (kWords >= 128) {
 #pragma unroll 1
       for (int c0 = 0; c0 < kWords; c0 += 128) {
-        Agg g[4];
+        Acc g[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-          agg_init(g[q]);
+          acc_init(g[q]);
         int m = 0;
         for (; m + 2 <= j; m += 2) {
           const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
           const uint32_t c_b = __shfl_sync(0xffffffffu, child, m + 1);
           const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
           const uint4 b = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_b) << LB)) + (c0 >> 2) + lane);
-          agg_add2(g[0], a.x, b.x);
-          agg_add2(g[1], a.y, b.y);
-          agg_add2(g[2], a.z, b.z);
-          agg_add2(g[3], a.w, b.w);
+          acc_add2(g[0], a.x, b.x);
+          acc_add2(g[1], a.y, b.y);
+          acc_add2(g[2], a.z, b.z);
+          acc_add2(g[3], a.w, b.w);
         }
         if (m < j) {
           const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
           const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
-          agg_add1(g[0], a.x);
-          agg_add1(g[1], a.y);
-          agg_add1(g[2], a.z);
-          agg_add1(g[3], a.w);
+          acc_add1(g[0], a.x);
+          acc_add1(g[1], a.y);
+          acc_add1(g[2], a.z);
+          acc_add1(g[3], a.w);
         }
-        reinterpret_cast<uint4*>(MN + c0)[lane] =
-            make_uint4(pack16(g[0].mnl, g[0].mnh), pack16(g[1].mnl, g[1].mnh), pack16(g[2].mnl, g[2].mnh),
-                       pack16(g[3].mnl, g[3].mnh));
-        reinterpret_cast<uint4*>(MX + c0)[lane] =
-            make_uint4(pack16(g[0].mxl, g[0].mxh), pack16(g[1].mxl, g[1].mxh), pack16(g[2].mxl, g[2].mxh),
-                       pack16(g[3].mxl, g[3].mxh));
-        reinterpret_cast<uint4*>(CT + c0)[lane] = make_uint4(g[0].ct, g[1].ct, g[2].ct, g[3].ct);
+        reinterpret_cast<uint4*>(OR + c0)[lane] = make_uint4(g[0].o, g[1].o, g[2].o, g[3].o);
+        reinterpret_cast<uint4*>(AND + c0)[lane] = make_uint4(g[0].a, g[1].a, g[2].a, g[3].a);
+        reinterpret_cast<uint4*>(CT + c0)[lane] = make_uint4(g[0].d, g[1].d, g[2].d, g[3].d);
       }
     } else {
       for (int w = lane; w < kWords; w += 32) {
-        Agg g;
-        agg_init(g);
+        Acc g;
+        acc_init(g);
         for (int m = 0; m < j; ++m) {
           const uint32_t c_a = __shfl_sync(__activemask(), child, m);
-          agg_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(table + (size_t(c_a) << LB)) + w));
+          acc_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(table + (size_t(c_a) << LB)) + w));
         }
-        MN[w] = pack16(g.mnl, g.mnh);
-        MX[w] = pack16(g.mxl, g.mxh);
-        CT[w] = g.ct;
+        OR[w] = g.o;
+        AND[w] = g.a;
+        CT[w] = g.d;
       }
     }
     __syncwarp();
@@ -324,51 +318,52 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       const uint32_t count = binom[kWordBits][s];
       for (uint32_t e = lane; e < count; e += 32) {
         const uint32_t w = sOrder[start + e];
-        const uint32_t mnp = MN[w], mxp = MX[w];
-        Agg g;
-        g.mnl = lo16(mnp);
-        g.mnh = hi16(mnp);
-        g.mxl = lo16(mxp);
-        g.mxh = hi16(mxp);
-        g.ct = CT[w];
+        Acc g;
+        g.o = OR[w];
+        g.a = AND[w];
+        g.d = CT[w];
         uint32_t r = w;
         for (; __popc(r) >= 2; r &= r - 1, r &= r - 1) {
           const uint32_t b1 = r & (0u - r);
           const uint32_t r2 = r & (r - 1);
-          agg_add2(g, T[w ^ b1], T[w ^ (r2 & (0u - r2))]);
+          acc_add2(g, T[w ^ b1], T[w ^ (r2 & (0u - r2))]);
         }
         if (r)
-          agg_add1(g, T[w ^ r]);
+          acc_add1(g, T[w ^ r]);
         const int k = j + s;
         if (k >= 3) {
-          const uint32_t ctl = lo16(g.ct), cth = hi16(g.ct);
-          // subset 00 (byte 0, lane 0 of the low half) is final first
-          uint32_t vl = resolve2(g.mnl, g.mxl, ctl);
-          const uint32_t b0 = vl & 0xFFu, f0 = b0 & 1u;
-          // fold it into subsets 10 (low half lane 1) and 01 (high half lane 0)
-          vl = resolve2(__vminu2(g.mnl, (b0 << 16) | 0xFFFFu), __vmaxu2(g.mxl, b0 << 16), ctl + (f0 << 16));
-          const uint32_t mnh = __vminu2(g.mnh, b0 | 0xFFFF0000u), mxh = __vmaxu2(g.mxh, b0);
-          uint32_t vh = resolve2(mnh, mxh, cth + f0);
-          // fold subsets 01 and 10 into 11 (high half lane 1)
-          const uint32_t b1 = vh & 0xFFu, b2 = vl >> 16;
-          vh = resolve2(__vminu2(mnh, (min(b1, b2) << 16) | 0xFFFFu), __vmaxu2(mxh, max(b1, b2) << 16),
-                        cth + f0 + (((b1 & 1u) + (b2 & 1u)) << 16));
-          T[w] = pack16(vl, vh);
+          // subset 00 (byte 0) is final first; fold it into 01 and 10
+          uint32_t v = resolve4(g);
+          const uint32_t x = __byte_perm(v, 0u, 0x4004u);
+          g.d |= g.o & x;
+          g.o |= x;
+          g.a &= x | 0xFF0000FFu;
+          // 01 and 10 (bytes 1, 2) are final; fold both into 11 (byte 3)
+          v = resolve4(g);
+          const uint32_t y1 = __byte_perm(v, 0u, 0x1444u), y2 = __byte_perm(v, 0u, 0x2444u);
+          g.d |= (g.o & (y1 | y2)) | (y1 & y2);
+          g.o |= y1 | y2;
+          g.a &= (y1 & y2) | 0x00FFFFFFu;
+          T[w] = resolve4(g);
         } else {
           // small subsets (|S| <= 2 possible): one byte at a time
-          const uint32_t mn = pack16(g.mnl, g.mnh), mx = pack16(g.mxl, g.mxh), ct = g.ct;
           const uint64_t S0 = Hfull | (uint64_t(w) << 2);
           const int n = G.n;
-          const uint32_t v0 = resolve(mn & 0xFFu, mx & 0xFFu, ct & 0xFFu, k, k == 2 && adjacent_in(adj, n, S0));
-          const uint32_t v1 = resolve(min((mn >> 8) & 0xFFu, v0), max((mx >> 8) & 0xFFu, v0),
-                                      ((ct >> 8) & 0xFFu) + (v0 & 1u), k + 1,
-                                      k + 1 == 2 && adjacent_in(adj, n, S0 | 1u));
-          const uint32_t v2 = resolve(min((mn >> 16) & 0xFFu, v0), max((mx >> 16) & 0xFFu, v0),
-                                      ((ct >> 16) & 0xFFu) + (v0 & 1u), k + 1,
-                                      k + 1 == 2 && adjacent_in(adj, n, S0 | 2u));
-          const uint32_t v3 = resolve(min(min(mn >> 24, v1), v2), max(max(mx >> 24, v1), v2),
-                                      (ct >> 24) + (v1 & 1u) + (v2 & 1u), k + 2,
-                                      k + 2 == 2 && adjacent_in(adj, n, S0 | 3u));
+          uint32_t o[4], a[4], d[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            o[q] = (g.o >> (8 * q)) & 0xFFu;
+            a[q] = (g.a >> (8 * q)) & 0xFFu;
+            d[q] = (g.d >> (8 * q)) & 0xFFu;
+          }
+          const uint32_t v0 = resolve1(o[0], a[0], d[0], k, k == 2 && adjacent_in(adj, n, S0));
+          fold1(o[1], a[1], d[1], v0);
+          fold1(o[2], a[2], d[2], v0);
+          const uint32_t v1 = resolve1(o[1], a[1], d[1], k + 1, k + 1 == 2 && adjacent_in(adj, n, S0 | 1u));
+          const uint32_t v2 = resolve1(o[2], a[2], d[2], k + 1, k + 1 == 2 && adjacent_in(adj, n, S0 | 2u));
+          fold1(o[3], a[3], d[3], v1);
+          fold1(o[3], a[3], d[3], v2);
+          const uint32_t v3 = resolve1(o[3], a[3], d[3], k + 2, k + 2 == 2 && adjacent_in(adj, n, S0 | 3u));
           T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
         }
       }
