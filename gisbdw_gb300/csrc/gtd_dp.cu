@@ -60,9 +60,11 @@ struct TileShape {
   static constexpr int kEntries = 1 << LB;
   static constexpr int kWords = kEntries / 4;   // 4 subsets per 32-bit word
   static constexpr int kWordBits = LB - 2;
-  // dynamic shared memory: per warp T, OR, AND, CT (kWords words each), then
-  // the shared word order (kWords uint16).
-  static constexpr size_t kPerWarp = size_t(4) * kWords * 4;
+  // dynamic shared memory: per warp T and U (kWords words each), then the
+  // word order shared by the CTA (kWords uint16). Between the two phases
+  // T and U hold the cross-tile children's summary as two virtual children
+  // (see the in-tile loop); T then receives the tile.
+  static constexpr size_t kPerWarp = size_t(2) * kWords * 4;
   static constexpr size_t kOrderOff = size_t(kDpWarps) * kPerWarp;
   static constexpr size_t kSmem = kOrderOff + kWords * 2;
 };
@@ -115,6 +117,15 @@ __device__ __forceinline__ void fold1(uint32_t& o, uint32_t& a, uint32_t& d, uin
   d |= o & v;
   o |= v;
   a &= v;
+}
+
+// A word's summary (o, a, d) of at least one child is reproduced by two
+// virtual children: o itself and a with bit 0 replaced by d. Their OR is o
+// (a's bits lie inside o's, d implies o's bit 0), their AND carries a's
+// treedepth bits, and both have bit 0 set exactly when d is: at least two
+// connected children.
+__device__ __forceinline__ uint32_t second_child(const Acc& c) {
+  return (c.a & 0xFEFEFEFEu) | (c.d & 0x01010101u);
 }
 
 // Level j, high part H and level offsets of local tile t of a graph with nh
@@ -207,9 +218,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   uint32_t* T = reinterpret_cast<uint32_t*>(smem + size_t(warp) * Shape::kPerWarp);
-  uint32_t* OR = T + kWords;
-  uint32_t* AND = OR + kWords;
-  uint32_t* CT = AND + kWords;
+  uint32_t* U = T + kWords;
   uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + Shape::kOrderOff);
   const Binom& binom = p.binom;
 
@@ -290,9 +299,9 @@ __global__ void __launch_bounds__(32 * kDpWarps)
           acc_add1(g[2], a.z);
           acc_add1(g[3], a.w);
         }
-        reinterpret_cast<uint4*>(OR + c0)[lane] = make_uint4(g[0].o, g[1].o, g[2].o, g[3].o);
-        reinterpret_cast<uint4*>(AND + c0)[lane] = make_uint4(g[0].a, g[1].a, g[2].a, g[3].a);
-        reinterpret_cast<uint4*>(CT + c0)[lane] = make_uint4(g[0].d, g[1].d, g[2].d, g[3].d);
+        reinterpret_cast<uint4*>(T + c0)[lane] = make_uint4(g[0].o, g[1].o, g[2].o, g[3].o);
+        reinterpret_cast<uint4*>(U + c0)[lane] =
+            make_uint4(second_child(g[0]), second_child(g[1]), second_child(g[2]), second_child(g[3]));
       }
     } else {
       for (int w = lane; w < kWords; w += 32) {
@@ -302,9 +311,8 @@ __global__ void __launch_bounds__(32 * kDpWarps)
           const uint32_t c_a = __shfl_sync(__activemask(), child, m);
           acc_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(table + (size_t(c_a) << LB)) + w));
         }
-        OR[w] = g.o;
-        AND[w] = g.a;
-        CT[w] = g.d;
+        T[w] = g.o;
+        U[w] = second_child(g);
       }
     }
     __syncwarp();
@@ -319,9 +327,9 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       for (uint32_t e = lane; e < count; e += 32) {
         const uint32_t w = sOrder[start + e];
         Acc g;
-        g.o = OR[w];
-        g.a = AND[w];
-        g.d = CT[w];
+        acc_init(g);
+        if (j > 0)  // the level-0 tile has no cross-tile children
+          acc_add2(g, T[w], U[w]);
         uint32_t r = w;
         for (; __popc(r) >= 2; r &= r - 1, r &= r - 1) {
           const uint32_t b1 = r & (0u - r);
