@@ -129,6 +129,14 @@ def test_dp_maximum_sizes(handle, port, n):
     assert port.edge_lower_bound(g.n, g.m) <= td <= port.heuristic(g, 0)[0]
     assert handle.dp_solve(G.path(n).adj64(), n)[0] == math.ceil(math.log2(n + 1))
     assert handle.dp_solve(G.cycle(n).adj64(), n)[0] == 1 + math.ceil(math.log2(n))
+    # treedepths above 32: the largest byte values and OR + AND sums the
+    # reduction meets (K_n: td n; K_n minus a perfect matching: td n - 1)
+    td, parent, _, _ = handle.dp_solve(G.complete(n).adj64(), n)
+    assert td == n and port.check_valid(G.complete(n), td, parent)
+    cp = G.Graph(n, [(u, v) for u in range(n) for v in range(u + 1, n) if not (u % 2 == 0 and v == u + 1)],
+                 name=f"cocktail{n}")
+    td, parent, _, _ = handle.dp_solve(cp.adj64(), n)
+    assert td == n - 1 and port.check_valid(cp, td, parent)
 
 
 def test_dp_closed_forms(handle):
