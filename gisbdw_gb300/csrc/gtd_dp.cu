@@ -60,13 +60,17 @@ struct TileShape {
   static constexpr int kEntries = 1 << LB;
   static constexpr int kWords = kEntries / 4;   // 4 subsets per 32-bit word
   static constexpr int kWordBits = LB - 2;
-  // dynamic shared memory: per warp T and U (kWords words each), then the
-  // word order shared by the CTA (kWords uint16). Between the two phases
-  // T and U hold the cross-tile children's summary as two virtual children
-  // (see the in-tile loop); T then receives the tile.
+  // dynamic shared memory: per warp T and U (kWords words each), then, for
+  // the CTA, the word order (kWords uint16) and a copy of the binomial
+  // table, then per warp the child-tile list (32 words). Between the two
+  // phases T and U hold the cross-tile children's summary as two virtual
+  // children (see the in-tile loop); T then receives the tile.
   static constexpr size_t kPerWarp = size_t(2) * kWords * 4;
   static constexpr size_t kOrderOff = size_t(kDpWarps) * kPerWarp;
-  static constexpr size_t kSmem = kOrderOff + kWords * 2;
+  static constexpr size_t kBinomOff = (kOrderOff + kWords * 2 + 15) & ~size_t(15);
+  static constexpr size_t kKidsOff = (kBinomOff + sizeof(uint32_t) * (kDpMaxHigh + 1) * (kDpMaxHigh + 1) + 15) &
+                                     ~size_t(15);
+  static constexpr size_t kSmem = kKidsOff + size_t(kDpWarps) * 32 * 4;
 };
 
 using Binom = uint32_t[kDpMaxHigh + 1][kDpMaxHigh + 1];
@@ -220,8 +224,12 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   uint32_t* T = reinterpret_cast<uint32_t*>(smem + size_t(warp) * Shape::kPerWarp);
   uint32_t* U = T + kWords;
   uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + Shape::kOrderOff);
+  Binom& sBinom = *reinterpret_cast<Binom*>(smem + Shape::kBinomOff);
+  uint32_t* kids = reinterpret_cast<uint32_t*>(smem + Shape::kKidsOff) + warp * 32;
   const Binom& binom = p.binom;
 
+  for (int i = threadIdx.x; i < (kDpMaxHigh + 1) * (kDpMaxHigh + 1); i += blockDim.x)
+    (&sBinom[0][0])[i] = (&binom[0][0])[i];
   // Word indices ordered by popcount, colex rank inside each popcount class.
   for (int w = threadIdx.x; w < kWords; w += blockDim.x) {
     const int i = __popc(w);
@@ -256,20 +264,34 @@ __global__ void __launch_bounds__(32 * kDpWarps)
 
     int j;
     uint32_t H, off_prev;
-    decode_tile(binom, G.nh, tl, j, H, off_prev);
+    decode_tile(sBinom, G.nh, tl, j, H, off_prev);
 
-    // Lane m < j owns child tile H - (m-th bit of H) and waits for it.
-    uint32_t child = 0;
+    // Lane v (a high vertex, v < nh <= 26) with v in H owns child tile
+    // H - v. Its colex rank keeps the terms C(u, i + 1) of the bits u < v and
+    // shifts the bits u > v down one place, C(u, i): a prefix sum and a
+    // suffix sum over the lanes. The child goes to kids[index of v in H].
+    const bool inH = (H >> lane) & 1u;
+    const uint32_t q = __popc(H & ((1u << lane) - 1u));
+    const uint32_t t1 = inH ? sBinom[lane][q + 1] : 0u, t0 = inH ? sBinom[lane][q] : 0u;
+    uint32_t pre = t1, suf = t0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t x = __shfl_up_sync(0xffffffffu, pre, d);
+      const uint32_t y = __shfl_down_sync(0xffffffffu, suf, d);
+      if (lane >= d)
+        pre += x;
+      if (lane + d < 32)
+        suf += y;
+    }
     bool ok = true;
-    if (lane < j) {
-      uint32_t rest = H;
-      for (int q = 0; q < lane; ++q)
-        rest &= rest - 1;
-      child = off_prev + rank_colex(binom, H & ~(rest & (0u - rest)));
+    if (inH) {
+      const uint32_t child = off_prev + (pre - t1) + (suf - t0);
+      kids[q] = child;
       ok = wait_flag(flags + child, p.epoch, p.timeout_ns, p.error);
     }
     if (__any_sync(0xffffffffu, !ok))
       break;
+    __syncwarp();  // kids[] written above, read by every lane below
 
     // Cross-tile children: j whole tiles, 4 subsets per word, children two
     // at a time.
@@ -282,8 +304,8 @@ __global__ void __launch_bounds__(32 * kDpWarps)
           acc_init(g[q]);
         int m = 0;
         for (; m + 2 <= j; m += 2) {
-          const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
-          const uint32_t c_b = __shfl_sync(0xffffffffu, child, m + 1);
+          const uint32_t c_a = kids[m];
+          const uint32_t c_b = kids[m + 1];
           const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
           const uint4 b = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_b) << LB)) + (c0 >> 2) + lane);
           acc_add2(g[0], a.x, b.x);
@@ -292,7 +314,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
           acc_add2(g[3], a.w, b.w);
         }
         if (m < j) {
-          const uint32_t c_a = __shfl_sync(0xffffffffu, child, m);
+          const uint32_t c_a = kids[m];
           const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
           acc_add1(g[0], a.x);
           acc_add1(g[1], a.y);
@@ -308,7 +330,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
         Acc g;
         acc_init(g);
         for (int m = 0; m < j; ++m) {
-          const uint32_t c_a = __shfl_sync(__activemask(), child, m);
+          const uint32_t c_a = kids[m];
           acc_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(table + (size_t(c_a) << LB)) + w));
         }
         T[w] = g.o;
