@@ -132,28 +132,33 @@ __device__ __forceinline__ uint32_t second_child(const Acc& c) {
   return (c.a & 0xFEFEFEFEu) | (c.d & 0x01010101u);
 }
 
-// Level j, high part H and level offsets of local tile t of a graph with nh
-// high vertices (level-major order, colex rank inside a level).
+// Level j, high part H and start of level j - 1 of local tile t of a graph
+// with nh high vertices (level-major order, colex rank inside a level),
+// computed by the whole warp: lane i <= nh holds the running level total
+// sum_{k <= i} C(nh, k) and a ballot counts the levels that end at or before
+// t; each element of H is then the largest a < nh with C(a, k) <= r (colex
+// unranking, one ballot per element, k = j .. 1).
 __device__ __forceinline__ void decode_tile(const Binom& binom, int nh, uint32_t t, int& j, uint32_t& H,
-                                            uint32_t& off_prev) {
-  uint32_t off = 0, prev = 0;
-  j = 0;
-  while (off + binom[nh][j] <= t) {
-    prev = off;
-    off += binom[nh][j];
-    ++j;
+                                                 uint32_t& off_prev) {
+  const int lane = threadIdx.x & 31;
+  uint32_t cum = lane <= nh ? binom[nh][lane] : 0u;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t x = __shfl_up_sync(0xffffffffu, cum, d);
+    if (lane >= d)
+      cum += x;
   }
-  off_prev = prev;
-  uint32_t r = t - off;
+  j = __popc(__ballot_sync(0xffffffffu, lane <= nh && cum <= t));
+  const uint32_t off = __shfl_sync(0xffffffffu, cum, (j + 31) & 31);       // lane j - 1
+  const uint32_t prev = __shfl_sync(0xffffffffu, cum, (j + 30) & 31);      // lane j - 2
+  off_prev = j >= 2 ? prev : 0u;
+  uint32_t r = t - (j >= 1 ? off : 0u);
   H = 0;
-  int k = j;
-  for (int a = nh - 1; k > 0; --a) {
-    const uint32_t c = binom[a][k];
-    if (r >= c) {
-      H |= 1u << a;
-      r -= c;
-      --k;
-    }
+  for (int k = j; k > 0; --k) {
+    const uint32_t c = lane < nh ? binom[lane][k] : 0xFFFFFFFFu;
+    const int a = 31 - __clz(__ballot_sync(0xffffffffu, c <= r));
+    H |= 1u << a;
+    r -= binom[a][k];
   }
 }
 
