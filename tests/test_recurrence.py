@@ -1,0 +1,237 @@
+"""CPU checks of the invariants the subset-DP kernel (gtd_dp.cu) relies on.
+
+* The bitwise recurrence: the children S - v of S have treedepth td(S) - 1
+  or td(S), so with s = OR(td) + AND(td) over the children,
+  td(S) = (s >> 1) + ((s & 1) | connected(S)); a third accumulator tracks
+  "at least two connected children". Restated here at the kernel's word
+  level (4 subsets per 32-bit word, byte = td << 1 | connected): the
+  cross-tile summary kept as two virtual children, the in-word order
+  00 -> 01, 10 -> 11 with byte permutes, the byte-at-a-time path for
+  |S| <= 2 and the level-0 tile. Checked against the oracle's tables
+  (DynamicCPU's values, dynamic_cpu.hpp / dynamic_gpu.cu:68-111).
+* The colex rank of H - v from per-bit terms (prefix and suffix sums), and
+  the warp-parallel tile decode (level by running totals, unranking one
+  element at a time), against the serial definitions (set_encoder.hpp:40-46).
+"""
+from math import comb
+
+import numpy as np
+import pytest
+
+from gisbdw_gb300 import graphs as G
+
+M32 = 0xFFFFFFFF
+
+
+def byte_perm(x, y, sel):
+    b = [(x >> (8 * i)) & 0xFF for i in range(4)] + [(y >> (8 * i)) & 0xFF for i in range(4)]
+    return sum(b[(sel >> (4 * i)) & 7] << (8 * i) for i in range(4))
+
+
+class Acc:
+    def __init__(self):
+        self.o, self.a, self.d = 0, M32, 0
+
+    def add2(self, x, y):
+        self.d |= (self.o & (x | y)) | (x & y)
+        self.o |= x | y
+        self.a &= x & y
+
+    def add1(self, x):
+        self.d |= self.o & x
+        self.o |= x
+        self.a &= x
+
+
+def resolve4(g):
+    s = ((g.o & 0xFEFEFEFE) + (g.a & 0xFEFEFEFE)) >> 1
+    cn = g.d & 0x01010101
+    return (((s & 0xFEFEFEFE) + (((s | cn) & 0x01010101) << 1)) | cn) & M32
+
+
+def resolve1(o, a, d, k, adjacent):
+    if k == 0:
+        return 0
+    cn = 1 if k == 1 else (int(adjacent) if k == 2 else d & 1)
+    s = ((o & 0xFE) + (a & 0xFE)) >> 1
+    return ((s & 0xFE) + (((s | cn) & 1) << 1)) | cn
+
+
+def second_child(g):
+    return (g.a & 0xFEFEFEFE) | (g.d & 0x01010101)
+
+
+def word_dp(g, lb):
+    """The kernel's schedule on one graph with tiles of 2^lb subsets; returns
+    the table indexed by subset mask (byte = td << 1 | connected)."""
+    n = g.n
+    adj = g.adjacency_masks()
+    nh = n - lb
+    words = 1 << (lb - 2)
+    tab = np.zeros(1 << n, dtype=np.int64)
+
+    def word_of(H, w):
+        base = (H << lb) | (w << 2)
+        return int(sum(int(tab[base + b]) << (8 * b) for b in range(4)))
+
+    for H in sorted(range(1 << nh), key=lambda h: (bin(h).count("1"), h)):
+        j = bin(H).count("1")
+        kids = [H & ~(1 << h) for h in range(nh) if H >> h & 1]
+        T, U = [0] * words, [0] * words
+        for w in range(words):
+            acc = Acc()
+            for m in range(0, len(kids) - 1, 2):
+                acc.add2(word_of(kids[m], w), word_of(kids[m + 1], w))
+            if len(kids) % 2:
+                acc.add1(word_of(kids[-1], w))
+            T[w], U[w] = acc.o, second_child(acc)
+        for s in range(lb - 1):
+            for w in (x for x in range(words) if bin(x).count("1") == s):
+                acc = Acc()
+                if j > 0:
+                    acc.add2(T[w], U[w])
+                for b in range(lb - 2):
+                    if w >> b & 1:
+                        acc.add1(T[w ^ (1 << b)])
+                k = j + s
+                if j > 0 and k >= 3:
+                    v = resolve4(acc)
+                    x = byte_perm(v, 0, 0x4004)
+                    acc.d |= acc.o & x
+                    acc.o |= x
+                    acc.a &= x | 0xFF0000FF
+                    v = resolve4(acc)
+                    y1, y2 = byte_perm(v, 0, 0x1444), byte_perm(v, 0, 0x2444)
+                    acc.d |= (acc.o & (y1 | y2)) | (y1 & y2)
+                    acc.o |= y1 | y2
+                    acc.a &= (y1 & y2) | 0x00FFFFFF
+                    T[w] = resolve4(acc)
+                else:
+                    S0 = (H << lb) | (w << 2)
+                    o = [(acc.o >> (8 * q)) & 0xFF for q in range(4)]
+                    a = [(acc.a >> (8 * q)) & 0xFF for q in range(4)]
+                    d = [(acc.d >> (8 * q)) & 0xFF for q in range(4)]
+
+                    def edge(S):
+                        u = (S & -S).bit_length() - 1
+                        v = S.bit_length() - 1
+                        return bool(adj[u] >> v & 1)
+
+                    def fold(q, val):
+                        d[q] |= o[q] & val
+                        o[q] |= val
+                        a[q] &= val
+                    v0 = resolve1(o[0], a[0], d[0], k, k == 2 and edge(S0))
+                    fold(1, v0)
+                    fold(2, v0)
+                    v1 = resolve1(o[1], a[1], d[1], k + 1, k + 1 == 2 and edge(S0 | 1))
+                    v2 = resolve1(o[2], a[2], d[2], k + 1, k + 1 == 2 and edge(S0 | 2))
+                    fold(3, v1)
+                    fold(3, v2)
+                    v3 = resolve1(o[3], a[3], d[3], k + 2, k + 2 == 2 and edge(S0 | 3))
+                    T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24)
+        for w in range(words):
+            for b in range(4):
+                tab[(H << lb) | (w << 2) | b] = (T[w] >> (8 * b)) & 0xFF
+    return tab
+
+
+def connected_flags(g):
+    adj = g.adjacency_masks()
+    out = np.zeros(1 << g.n, dtype=np.int64)
+    for S in range(1, 1 << g.n):
+        reach = frontier = S & -S
+        while frontier:
+            nb = 0
+            f = frontier
+            while f:
+                b = f & -f
+                nb |= adj[b.bit_length() - 1]
+                f ^= b
+            frontier = nb & S & ~reach
+            reach |= frontier
+        out[S] = int(reach == S)
+    return out
+
+
+GRAPHS = [G.gnp_connected(9, 0.3, 1), G.gnp_connected(10, 0.5, 2), G.sparse_connected(10, 3), G.grid(2, 5),
+          G.complete(8), G.path(9), G.cycle(10), G.star(9),
+          G.Graph(10, [(0, 1), (2, 3), (3, 4), (6, 7), (7, 8), (8, 6)], name="forest10"),
+          G.Graph(8, [], name="empty8")]
+
+
+@pytest.mark.parametrize("lb", [4, 6])
+def test_word_level_recurrence_matches_oracle(port, lb):
+    for g in GRAPHS:
+        tab = word_dp(g, lb)
+        assert np.array_equal(tab >> 1, port.dp_table(g)), (g.name, lb)
+        conn = connected_flags(g)
+        assert np.array_equal(tab[1:] & 1, conn[1:]), (g.name, lb)
+
+
+def test_two_virtual_children_reproduce_the_summary():
+    rng = np.random.default_rng(0)
+    for _ in range(2000):
+        count = int(rng.integers(1, 9))
+        kids = [int(x) for x in rng.integers(0, 1 << 32, size=count, dtype=np.uint64)]
+        acc = Acc()
+        for x in kids:
+            acc.add1(x)
+        pair = Acc()
+        pair.add2(acc.o, second_child(acc))
+        assert pair.o == acc.o
+        assert pair.a & 0xFEFEFEFE == acc.a & 0xFEFEFEFE
+        assert pair.d & 0x01010101 == acc.d & 0x01010101
+
+
+def rank_colex(H):
+    r, q = 0, 0
+    while H:
+        b = (H & -H).bit_length() - 1
+        q += 1
+        r += comb(b, q)
+        H &= H - 1
+    return r
+
+
+def test_child_ranks_by_prefix_and_suffix_sums():
+    for nh in range(0, 11):
+        for H in range(1 << nh):
+            t1, t0 = [0] * 32, [0] * 32
+            for v in range(nh):
+                if H >> v & 1:
+                    q = bin(H & ((1 << v) - 1)).count("1")
+                    t1[v], t0[v] = comb(v, q + 1), comb(v, q)
+            for v in range(nh):
+                if H >> v & 1:
+                    assert sum(t1[:v]) + sum(t0[v + 1:]) == rank_colex(H & ~(1 << v))
+
+
+def test_warp_tile_decode_matches_serial():
+    def serial(nh, t):
+        off = prev = j = 0
+        while off + comb(nh, j) <= t:
+            prev, off, j = off, off + comb(nh, j), j + 1
+        r, H, k, a = t - off, 0, j, nh - 1
+        while k > 0:
+            if r >= comb(a, k):
+                H |= 1 << a
+                r -= comb(a, k)
+                k -= 1
+            a -= 1
+        return j, H, prev
+
+    def warp(nh, t):
+        cum = np.cumsum([comb(nh, i) if i <= nh else 0 for i in range(32)])
+        j = sum(1 for i in range(32) if i <= nh and cum[i] <= t)
+        off, prev = int(cum[(j + 31) & 31]), int(cum[(j + 30) & 31])
+        r, H = t - (off if j >= 1 else 0), 0
+        for k in range(j, 0, -1):
+            a = max(x for x in range(32) if (comb(x, k) if x < nh else M32) <= r)
+            H |= 1 << a
+            r -= comb(a, k)
+        return j, H, prev if j >= 2 else 0
+
+    for nh in range(0, 11):
+        for t in range(1 << nh):
+            assert serial(nh, t) == warp(nh, t), (nh, t)
