@@ -32,11 +32,14 @@
 //    32-bit word, words in popcount order of the word index.
 //  * Schedule. One persistent launch; every warp is an independent tile
 //    worker (no CTA barriers in the loop). A warp takes a tile by ticket
-//    (atomicAdd) in level-major order, its lanes wait on the ready flags of
-//    the |H| child tiles (each wait bounded by a deadline), the warp reduces
-//    the children with OR / AND / majority logic on 4-byte words, resolves
-//    the tile, stores it and publishes its flag. A tile only waits on tiles with smaller tickets,
-//    and a ticket is only taken by a running warp, so the smallest unfinished
+//    (atomicAdd) in level-major order and decodes it with ballots over a
+//    shared-memory binomial table; lane v in H ranks child tile H - v by a
+//    prefix and a suffix sum and waits on its ready flag (each wait bounded
+//    by a deadline). The warp reduces the cross-tile children with OR / AND /
+//    majority logic on 16-byte loads, keeps that summary as two virtual
+//    children in shared memory, resolves the tile there, stores it and
+//    publishes its flag. A tile only waits on tiles with smaller tickets, and
+//    a ticket is only taken by a running warp, so the smallest unfinished
 //    ticket can always proceed.
 //
 // Reconstruction (dp_tree_kernel): one warp, one lane per vertex, rebuilds
