@@ -8,6 +8,7 @@ from __future__ import annotations
 import ctypes
 import os
 import threading
+from collections.abc import Sequence
 from typing import Optional, Tuple
 
 import numpy as np
@@ -213,8 +214,7 @@ class Handle:
         stats = BatchStats()
         self._check(self.L.gtd_dp_solve_batch(self._h, ctypes.cast(descs, _vp), count, _ptr(pool), pool.size,
                                               _ptr(td), _ptr(parent), ctypes.byref(opts), ctypes.byref(stats)))
-        parents = [parent[d.offset:d.offset + d.n] for d in descs]
-        return td, parents, stats.as_dict()
+        return td, PerGraph(parent, descs), stats.as_dict()
 
     def dp_solve_batch_device(self, descs, count: int, d_pool: int, pool_len: int, d_td: int, d_parent: int,
                               tile_bits: int = 0, ctas_per_sm: int = 0, timeout_ns: int = 0,
@@ -246,6 +246,30 @@ class Handle:
         out = np.empty(nbytes, dtype=np.uint8)
         self._check(self.L.gtd_dp_read_table(self._h, _ptr(out), nbytes))
         return out, n, lb
+
+
+class PerGraph(Sequence):
+    """Per-graph views into one flat result array (parents of a batch), made
+    on access: the batch call returns without building thousands of views.
+    Indexing gives an array view; a slice gives a list of views."""
+    __slots__ = ("_flat", "_off", "_n")
+
+    def __init__(self, flat, descs):
+        self._flat = flat
+        if len(descs):
+            arr = np.ctypeslib.as_array(descs)
+            self._off, self._n = arr["offset"].tolist(), arr["n"].tolist()
+        else:
+            self._off, self._n = [], []
+
+    def __len__(self):
+        return len(self._off)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[k] for k in range(*i.indices(len(self)))]
+        o = self._off[i]
+        return self._flat[o:o + self._n[i]]
 
 
 def pack_batch(graphs):
