@@ -129,6 +129,11 @@ def test_dp_maximum_sizes(handle, port, n):
     assert port.edge_lower_bound(g.n, g.m) <= td <= port.heuristic(g, 0)[0]
     assert handle.dp_solve(G.path(n).adj64(), n)[0] == math.ceil(math.log2(n + 1))
     assert handle.dp_solve(G.cycle(n).adj64(), n)[0] == 1 + math.ceil(math.log2(n))
+    if n == 34:
+        # 8-bit tiles: 26 high vertices, the most the tile map allows (every
+        # lane of the warp decode and child ranking in use)
+        td8, parent8, _, _ = handle.dp_solve(g.adj64(), g.n, tile_bits=8)
+        assert td8 == td and parent8.tolist() == parent.tolist()
     # treedepths above 32: the largest byte values and OR + AND sums the
     # reduction meets (K_n: td n; K_n minus a perfect matching: td n - 1)
     td, parent, _, _ = handle.dp_solve(G.complete(n).adj64(), n)
