@@ -163,16 +163,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def ncu_bytes_per_subset():
-    """DRAM bytes per subset of the DP tile kernel, measured by ncu on an
-    n = 28 launch (profiles/dp_tile_kernel.md, line 'dram_bytes_per_subset')."""
+def ncu_profile_figure(key):
+    """A figure of the DP tile kernel's ncu capture on an n = 28 launch
+    (profiles/dp_tile_kernel.md, line '<key>: <value>')."""
     path = os.path.join(ROOT, "profiles", "dp_tile_kernel.md")
     try:
         text = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_subset:\s*([0-9.eE+]+)", text)
+    m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
+
+
+def ncu_bytes_per_subset():
+    """DRAM bytes per subset of the DP tile kernel (ncu, n = 28 launch)."""
+    return ncu_profile_figure("dram_bytes_per_subset")
 
 
 def cpu_model():
@@ -497,6 +502,7 @@ def run_gpu(args, graphs):
                                   "shared memory and most cross-tile children from L2, so DRAM moves about "
                                   "1.1 B per subset (traffic) and frac can exceed 1; the kernel is bound "
                                   "by instruction issue",
+                     "issue_active_frac_ncu": ncu_profile_figure("issue_active_frac"),
                      "alg_bytes_per_launch_mean": alg / launches,
                      "launch_ms_mean": kms / launches, "by_n": by_n_out},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
