@@ -77,9 +77,43 @@ constexpr int kBnbWarps = 4;
 constexpr int kMaxComps = 40;            // components with >= 3 vertices: <= 104 / 3
 constexpr int kMemoProbes = 8;
 constexpr int kMmdMin = 10;              // minor-min-width bound for |C| >= this
-constexpr int kSubsetMin = 16;
-constexpr int kMiniMin = 6, kMiniMax = 10;  // components decided exactly by a subset DP           // memo bounds of the C - v for |C| >= this
+constexpr int kSubsetMin = 16;           // memo bounds of the C - v for |C| >= this
+constexpr int kMiniMin = 6, kMiniMax = 10;  // components decided exactly by a subset DP
 constexpr uint32_t kSeedRoot = 0xFFu;
+
+// The subsets of kMiniMax vertices grouped by size, increasing bit masks
+// inside a group. Increasing masks are colex order, so for a component of
+// m <= kMiniMax vertices the first C(m, l) masks of group l are exactly its
+// l-subsets: the small-component DP walks each level without skipping.
+struct MiniOrder {
+  uint16_t subset[1 << kMiniMax];
+  uint16_t start[kMiniMax + 2];
+  uint16_t count[kMiniMax + 1][kMiniMax + 1];  // count[m][l] = C(m, l)
+};
+
+constexpr MiniOrder make_mini_order() {
+  MiniOrder o{};
+  int pos = 0;
+  for (int l = 0; l <= kMiniMax; ++l) {
+    o.start[l] = static_cast<uint16_t>(pos);
+    for (int S = 0; S < (1 << kMiniMax); ++S) {
+      int c = 0;
+      for (int x = S; x; x &= x - 1)
+        ++c;
+      if (c == l)
+        o.subset[pos++] = static_cast<uint16_t>(S);
+    }
+  }
+  o.start[kMiniMax + 1] = static_cast<uint16_t>(pos);
+  for (int m = 0; m <= kMiniMax; ++m) {
+    o.count[m][0] = 1;
+    for (int l = 1; l <= kMiniMax; ++l)
+      o.count[m][l] = m == 0 ? 0 : static_cast<uint16_t>(o.count[m - 1][l - 1] + o.count[m - 1][l]);
+  }
+  return o;
+}
+
+static __device__ const MiniOrder kMiniOrder = make_mini_order();
 constexpr int kUnknownUb = 127;
 constexpr int kIoUnfinished = 3;         // d_io word: items that spent their budget this round
 constexpr int kIoExited = 200;           // d_io word: warps that left the current pass
@@ -342,9 +376,9 @@ struct Search {
     uint8_t* T = mini;
     const uint32_t full = (1u << m) - 1u;
     for (int l = 1; l <= m; ++l) {
-      for (uint32_t S = lane; S <= full; S += 32) {
-        if (__popc(S) != l)
-          continue;
+      const int level_size = kMiniOrder.count[m][l], base = kMiniOrder.start[l];
+      for (int e = lane; e < level_size; e += 32) {
+        const uint32_t S = kMiniOrder.subset[base + e];
         uint32_t b;
         if (l == 1) {
           b = 3u;  // td 1, connected
