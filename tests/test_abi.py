@@ -68,3 +68,21 @@ def test_create_without_gpu_fails_cleanly():
     h = ctypes.c_void_p()
     st = L.gtd_create(ctypes.byref(h), 0, None)
     assert st in (1, 6) and not h.value
+
+
+def test_batch_parents_are_per_graph_views():
+    """dp_solve_batch hands back the flat parent pool as per-graph views made
+    on access: indexing, negative indices, slices and iteration agree with
+    the descriptors' offsets, and an empty batch is an empty sequence."""
+    from gisbdw_gb300 import graphs as G
+    gs = [G.path(5), G.cycle(7), G.complete(3), G.grid(2, 3)]
+    descs, pool = _lib.pack_batch(gs)
+    flat = np.arange(pool.size, dtype=np.int32)
+    pg = _lib.PerGraph(flat, descs)
+    want = [flat[d.offset:d.offset + d.n] for d in descs]
+    assert len(pg) == len(gs)
+    assert all(np.array_equal(a, b) for a, b in zip(pg, want))
+    assert np.array_equal(pg[-1], want[-1])
+    assert [x.tolist() for x in pg[1::2]] == [x.tolist() for x in want[1::2]]
+    assert np.shares_memory(pg[0], flat)
+    assert len(_lib.PerGraph(flat, (_lib.GraphDesc * 0)())) == 0
