@@ -24,7 +24,11 @@ Arms:
                      region).
   --impl reference   the reference's CPU algorithm (the oracle restatement of
                      DynamicGPU's recurrence, dynamic_gpu.cu:68-112, on all
-                     host threads), each step one graph of a bounded sample.
+                     host threads) on the same 9 graphs: each step solves one
+                     graph (table, tree, elimination order), cycling through
+                     all of them, and the rate is the workload's 9 graphs over
+                     the sum of their mean times. The ``config`` object is the
+                     same in both arms.
 
 Prints one JSON line (rank 0).
 """
@@ -195,22 +199,64 @@ def cpu_model():
 # CPU legs (the oracle is loaded only here).
 # ---------------------------------------------------------------------------
 
+def config_c2(graphs):
+    """The workload's config object, identical in both arms."""
+    return {"workload": WORKLOAD_C2, "graphs": [g.name for g in graphs],
+            "l2": "working set (DP tables 256 MiB-4 GiB) > L2"}
+
+
 def cpu_sample_graphs(graphs):
-    return [g for g in graphs if g.n == 28]
+    """One graph of each vertex count of the workload (the bounded sample of
+    the GPU arm's CPU baseline)."""
+    seen, out = set(), []
+    for g in graphs:
+        if g.n not in seen:
+            seen.add(g.n)
+            out.append(g)
+    return out
 
 
-def time_cpu_dp(graphs, steps, threads):
+def workload_rate(graphs, samples):
+    """Solves/s of the whole workload from per-graph CPU times: the workload's
+    graph count over the sum of each graph's mean time; a graph that was not
+    timed takes the mean time of the timed graphs with its vertex count."""
+    by_name, by_n = {}, {}
+    for g, t in samples:
+        by_name.setdefault(g.name, []).append(t)
+        by_n.setdefault(g.n, []).append(t)
+    total = 0.0
+    for g in graphs:
+        ts = by_name.get(g.name) or by_n.get(g.n)
+        if not ts:
+            return None
+        total += statistics.mean(ts)
+    return len(graphs) / total
+
+
+def cpu_dp_solve(port, g, threads):
+    """The oracle's restatement of DynamicGPU (dynamic_gpu.cu:68-112: the
+    all-subsets table), its tree (dynamic_cpu.hpp:59-81) and GetElimination
+    order (dynamic_gpu.hpp:48-64) for one graph: (td, parent, order)."""
+    T = port.dp_table(g, nthreads=threads)
+    td, par = port.tree_from_table(g, T)
+    order = port.get_elimination(g, T, (1 << g.n) - 1)
+    del T
+    return td, par, order
+
+
+def time_cpu_dp(graphs, steps, threads, start=0):
+    """Steps of one graph each, cycling through `graphs` from index `start`:
+    [(graph, seconds, (td, parent, order))]."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     port = oracle.Port()
-    times, tds = [], []
+    out = []
     for i in range(steps):
-        g = graphs[i % len(graphs)]
+        g = graphs[(start + i) % len(graphs)]
         t0 = time.perf_counter()
-        td, _ = port.dp_solve(g, nthreads=threads)
-        times.append(time.perf_counter() - t0)
-        tds.append(td)
-    return times, tds
+        res = cpu_dp_solve(port, g, threads)
+        out.append((g, time.perf_counter() - t0, res))
+    return out
 
 
 def time_cpu_bnb(graphs, node_limit, threads):
@@ -234,24 +280,32 @@ def time_cpu_bnb(graphs, node_limit, threads):
 
 
 def run_reference(args, graphs):
+    """The reference's algorithm for this workload on the host cores: every
+    step solves one graph of the workload (table, tree and elimination order),
+    cycling through all of them; the rate is the whole workload's (its graph
+    count over the sum of the graphs' mean times), so both arms report the
+    same quantity on the same graphs."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = cpu_sample_graphs(graphs)
-    time_cpu_dp(sample, args.warmup, threads)
-    times, _ = time_cpu_dp(sample, args.steps, threads)
-    total = sum(times)
-    value = len(times) / total
-    desc = (f"n=28 graphs of the workload ({', '.join(g.name for g in sample)}), one per step, "
-            f"oracle restatement of DynamicGPU's all-subsets recurrence on {threads} host threads")
+    small = [g for g in graphs if g.n == min(x.n for x in graphs)]
+    time_cpu_dp(small, args.warmup, threads)  # warm-up on the smallest graphs
+    res = time_cpu_dp(graphs, args.steps, threads)
+    samples = [(g, t) for g, t, _ in res]
+    value = workload_rate(graphs, samples)
+    timed = sorted({g.name for g, _ in samples})
+    desc = (f"all {len(graphs)} graphs of the workload, one per step in turn ({len(timed)} timed); "
+            f"oracle restatement of DynamicGPU's all-subsets recurrence (dynamic_gpu.cu:68-112) with the "
+            f"tree and GetElimination order, on {threads} host threads; rate = graphs / sum of per-graph "
+            f"mean times")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000 * total / len(times), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": WORKLOAD_C2, "l2": "working set (DP tables 256 MiB-4 GiB) > L2",
-                   "parallelism": "host threads"},
+        "ms_per_step": 1000 * sum(t for _, t in samples) / len(samples), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": config_c2(graphs), "parallelism": f"{threads} host threads",
+        "per_graph_s": {name: statistics.mean(t for g, t in samples if g.name == name) for name in timed},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
                          "sample": desc, "cpu": cpu_model()},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -276,7 +330,14 @@ def measure_dp_c3(h, steps, warmup, count=4096):
     tune_s = time.perf_counter() - t0
     for _ in range(warmup):
         td, pars, st = h.dp_solve_batch(graphs, packed=packed)
-    bad = [g.name for g, t, p in zip(graphs[::64], td[::64], pars[::64]) if not check_tree(g, int(t), p)]
+    # every graph: a valid tree of height td, and the same td and parent array
+    # as the single-graph entry point (a separate launch path and layout)
+    bad = [g.name for g, t, p in zip(graphs, td, pars) if not check_tree(g, int(t), p)]
+    single_differs = []
+    for g, t, p in zip(graphs, td, pars):
+        std, spar, _, _ = h.dp_solve(g.adj64(), g.n, want_order=False)
+        if std != int(t) or spar.tolist() != p.tolist():
+            single_differs.append(g.name)
     dev, host = [], []
     for _ in range(steps):
         t0 = time.perf_counter()
@@ -289,9 +350,10 @@ def measure_dp_c3(h, steps, warmup, count=4096):
             "e2e_solves_per_s": len(graphs) / statistics.median(host), "alg_bytes": st["alg_bytes"],
             "alg_GBps": st["alg_bytes"] / (ms / 1e3) / 1e9, "frac_of_" + peak_kind + "_hbm":
             st["alg_bytes"] / (ms / 1e3) / 1e9 / peak, "tile_bits": st["tile_bits"], "ctas": st["ctas"],
-            "cuda_graph_replayed": bool(st["graph_replayed"]), "trees_checked": len(graphs[::64]),
-            "autotune_s": tune_s, "autotune_best_bits_n24": int(8 + rates[-1].argmax()),
-            "trees_invalid": bad}
+            "cuda_graph_replayed": bool(st["graph_replayed"]), "trees_checked": len(graphs),
+            "trees_invalid": bad, "td_parent_equal_to_single_solves": not single_differs,
+            "differs_from_single": single_differs[:8],
+            "autotune_s": tune_s, "autotune_best_bits_n24": int(8 + rates[-1].argmax())}
 
 
 def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_nodes=0, family="c4"):
@@ -449,7 +511,6 @@ def run_gpu(args, graphs):
     elapsed_ms = elapsed_s * 1000.0
 
     # e2e: host buffers through the C ABI call (adjacency H2D, results D2H)
-    e2e_times = []
     h2d = sum(8 * g.n for g in graphs)
     d2h = len(graphs) * (136 * 4)
     adjs = [g.adj64() for g in graphs]
@@ -457,10 +518,11 @@ def run_gpu(args, graphs):
         for i, g in enumerate(graphs):
             h.dp_solve(adjs[i], g.n, tile_bits=args.tile_bits)
     barrier()
+    gpu_out = {}
     t0 = time.perf_counter()
     for _ in range(args.steps):
         for i, g in enumerate(graphs):
-            td, par, order, _ = h.dp_solve(adjs[i], g.n, tile_bits=args.tile_bits)
+            gpu_out[g.name] = h.dp_solve(adjs[i], g.n, tile_bits=args.tile_bits)[:3]
     e2e_s = time.perf_counter() - t0
     barrier()
     e2e_value, _ = job_rate(len(graphs) * args.steps, e2e_s, world)
@@ -487,22 +549,21 @@ def run_gpu(args, graphs):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD_C2,
-                   "graphs": [g.name for g in graphs], "l2": "working set (DP tables 256 MiB-4 GiB) > L2",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "config": config_c2(graphs), "parallelism": "replicas" if world > 1 else "1 GPU",
         "p50_time_to_proof_ms": statistics.median(per_graph_ms),
         "treedepths": tds,
         "roofline": {"bound": "hbm", "kernel": "dp_tile_kernel", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
-                     "traffic_note": "ncu DRAM read+write bytes of an n=28 launch per subset, scaled by 2^n "
-                                     "and averaged over the workload's launches",
+                     "traffic_note": "profiled constant, not measured in this run: ncu DRAM read+write bytes "
+                                     "per subset of one n=28 launch (profiles/dp_tile_kernel.md), scaled by "
+                                     "2^n and averaged over the workload's launches",
                      "frac_note": "achieved counts 1 + n/2 algorithmic bytes per subset (one written, one "
                                   "gathered per child); the tile layout serves the in-tile children from "
                                   "shared memory and most cross-tile children from L2, so DRAM moves about "
                                   "1.1 B per subset (traffic) and frac can exceed 1; the kernel is bound "
                                   "by instruction issue",
-                     "issue_active_frac_ncu": ncu_profile_figure("issue_active_frac"),
+                     "issue_active_frac_profiled_n28": ncu_profile_figure("issue_active_frac"),
                      "alg_bytes_per_launch_mean": alg / launches,
                      "launch_ms_mean": kms / launches, "by_n": by_n_out},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
@@ -518,13 +579,23 @@ def run_gpu(args, graphs):
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample = cpu_sample_graphs(graphs)
-        times, ctds = time_cpu_dp(sample, len(sample), threads)
-        gpu_td = {g.name: tds[i] for i, g in enumerate(graphs)}
+        res = time_cpu_dp(sample, len(sample), threads)
+        same = {}
+        for g, _, (ctd, cpar, corder) in res:
+            gtd, gpar, gorder = gpu_out[g.name]
+            same[g.name] = {"td": ctd == gtd, "parent": cpar.tolist() == gpar.tolist(),
+                            "order": corder == gorder.tolist()}
         line["cpu_baseline"] = {
-            "value": len(times) / sum(times), "unit": "solves/s", "cores": threads, "kind": "port",
-            "sample": f"{len(sample)} n=28 graphs of the workload, oracle restatement of DynamicGPU's "
-                      f"recurrence on {threads} host threads ({cpu_model()})",
-            "td_agree": all(gpu_td[g.name] == t for g, t in zip(sample, ctds))}
+            "value": workload_rate(graphs, [(g, t) for g, t, _ in res]), "unit": "solves/s", "cores": threads,
+            "kind": "port",
+            "sample": f"one graph per vertex count ({', '.join(g.name for g in sample)}), each solved once "
+                      f"(table, tree, GetElimination order) by the oracle restatement of DynamicGPU's "
+                      f"recurrence on {threads} host threads ({cpu_model()}); rate = the workload's "
+                      f"{len(graphs)} graphs over the sum of their times, each graph taking the time of the "
+                      f"sampled graph with its vertex count",
+            "per_graph_s": {g.name: t for g, t, _ in res},
+            "parity_bit_exact": all(all(v.values()) for v in same.values()),
+            "parity": same}
     if rank == 0:
         print(json.dumps(line), flush=True)
     h.close()

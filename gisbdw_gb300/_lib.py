@@ -127,12 +127,27 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                                 ctypes.POINTER(BatchOpts)]
         L.gtd_dp_batch_sync.argtypes = [_vp, ctypes.POINTER(BatchStats)]
         L.gtd_dp_autotune.argtypes = [_vp, _i, _i, _vp]
+        L.gtd_abort.argtypes = [_vp]
+        L.gtd_inject_fault.argtypes = [_i, _i]
         _LIB = L
         return L
 
 
 def _ptr(a: np.ndarray) -> ctypes.c_void_p:
     return a.ctypes.data_as(_vp)
+
+
+FAULT_NONE, FAULT_ALLOC, FAULT_STALL = 0, 1, 2
+
+
+def inject_fault(kind: int, count: int = 1) -> None:
+    """gtd_inject_fault (tests of the error paths): FAULT_ALLOC makes the
+    count-th device allocation from now fail (GTD_OOM); FAULT_STALL makes the
+    next count single-graph DP solves wait on a tile nothing computes
+    (GTD_TIMEOUT); FAULT_NONE clears both."""
+    st = load().gtd_inject_fault(kind, count)
+    if st != 0:
+        raise _error(st, "gtd_inject_fault")
 
 
 class Handle:
@@ -148,6 +163,11 @@ class Handle:
     def _check(self, st: int) -> None:
         if st != 0:
             raise _error(st, self.L.gtd_last_error(self._h).decode())
+
+    def abort(self) -> None:
+        """gtd_abort: stops the call running on this handle (from another
+        thread); that call raises GtdError with GTD_ABORTED."""
+        self._check(self.L.gtd_abort(self._h))
 
     def close(self) -> None:
         if self._h:

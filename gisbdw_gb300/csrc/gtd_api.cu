@@ -3,6 +3,7 @@
 // gtd_status and keeps a message for gtd_last_error.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -62,6 +63,29 @@ gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info) {
   }
 }
 
+namespace {
+std::atomic<int> g_alloc_faults{0};  // pending: the n-th allocation from now fails (0 = none)
+std::atomic<int> g_stall_faults{0};  // pending: DP launches that skip their first tile
+}  // namespace
+
+bool take_alloc_fault() {
+  int n = g_alloc_faults.load();
+  while (n > 0) {
+    if (g_alloc_faults.compare_exchange_weak(n, n - 1))
+      return n == 1;
+  }
+  return false;
+}
+
+bool take_stall_fault() {
+  int n = g_stall_faults.load();
+  while (n > 0) {
+    if (g_stall_faults.compare_exchange_weak(n, n - 1))
+      return true;
+  }
+  return false;
+}
+
 cudaError_t ensure_device(void** ptr, size_t* cap, size_t bytes) {
   if (*cap >= bytes && *ptr)
     return cudaSuccess;
@@ -70,6 +94,8 @@ cudaError_t ensure_device(void** ptr, size_t* cap, size_t bytes) {
   *ptr = nullptr;
   *cap = 0;
   const size_t want = bytes < 256 ? 256 : bytes;
+  if (take_alloc_fault())
+    return cudaErrorMemoryAllocation;
   cudaError_t e = cudaMalloc(ptr, want);
   if (e == cudaSuccess)
     *cap = want;
@@ -79,12 +105,8 @@ cudaError_t ensure_device(void** ptr, size_t* cap, size_t bytes) {
 gtd_status ensure_flags(gtd_handle h, size_t tiles) {
   if (h->flags_cap >= tiles && h->d_flags)
     return GTD_OK;
-  size_t cap_bytes = h->flags_cap * sizeof(uint32_t);
-  void* p = h->d_flags;
-  GTD_CUDA(h, ensure_device(&p, &cap_bytes, tiles * sizeof(uint32_t)));
-  h->d_flags = static_cast<uint32_t*>(p);
-  h->flags_cap = cap_bytes / sizeof(uint32_t);
-  GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, cap_bytes, h->stream));
+  GTD_CUDA(h, ensure_field(&h->d_flags, &h->flags_cap, tiles));
+  GTD_CUDA(h, cudaMemsetAsync(h->d_flags, 0, h->flags_cap * sizeof(uint32_t), h->stream));
   h->epoch = 0;
   return GTD_OK;
 }
@@ -114,9 +136,7 @@ gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_o
   const size_t table_bytes = size_t(1) << n;
   if (h->table_cap < table_bytes)
     h->have_table = false;
-  void* tp = h->d_table;
-  GTD_CUDA(h, ensure_device(&tp, &h->table_cap, table_bytes));
-  h->d_table = static_cast<uint8_t*>(tp);
+  GTD_CUDA(h, ensure_field(&h->d_table, &h->table_cap, table_bytes));
   gtd_status s = ensure_flags(h, L.ntiles);
   if (s != GTD_OK)
     return s;
@@ -156,6 +176,8 @@ gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_o
     ctas = p.total_tiles;
 
   GTD_CUDA(h, cudaMemsetAsync(h->d_io, 0, 4 * sizeof(int32_t), h->stream));
+  if (take_stall_fault())  // test injection: ticket 0 (the level-0 tile) is never taken
+    GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoTicket, 1, 1, h->stream));
   GTD_CUDA(h, dp_launch_validate(p, h->stream));
   GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
   GTD_CUDA(h, dp_launch_tiles(p, static_cast<int>(ctas), h->stream));
@@ -233,6 +255,8 @@ gtd_status gtd_create(gtd_handle* out, int device, void* stream) {
       h->own_stream = true;
     }
   }
+  if (e == cudaSuccess)
+    e = cudaStreamCreateWithFlags(&h->abort_stream, cudaStreamNonBlocking);
   for (int i = 0; i < 4 && e == cudaSuccess; ++i)
     e = cudaEventCreate(&h->ev[i]);
   if (e == cudaSuccess)
@@ -283,6 +307,8 @@ gtd_status gtd_destroy(gtd_handle h) {
         cudaEventDestroy(e);
     if (h->own_stream && h->stream)
       cudaStreamDestroy(h->stream);
+    if (h->abort_stream)
+      cudaStreamDestroy(h->abort_stream);
   }
   delete h;
   return GTD_OK;
@@ -317,7 +343,7 @@ gtd_status gtd_dp_solve(gtd_handle h, const uint64_t* adj, int n, int32_t* td_ou
   s = dp_enqueue(h, h->d_adj, n, opts, h->d_io + kIoTd, h->d_io + kIoParent, h->d_io + kIoOrder);
   if (s != GTD_OK)
     return s;
-  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
+  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + kPinnedIo);
   GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, (kIoOrder + 64) * sizeof(int32_t), cudaMemcpyDeviceToHost,
                               h->stream));
   GTD_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -354,7 +380,7 @@ gtd_status gtd_sync(gtd_handle h, gtd_dp_stats* stats) {
   if (!h)
     return GTD_INVALID_ARG;
   DeviceGuard g(h->device);
-  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
+  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + kPinnedIo);
   GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
   GTD_CUDA(h, cudaStreamSynchronize(h->stream));
   collect_stats(h);
@@ -388,7 +414,7 @@ gtd_status gtd_dp_query(gtd_handle h, uint64_t subset_mask, int32_t* td_out, int
   p.order_out = order_out ? h->d_io + kIoOrder : nullptr;
   GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoError, 0, 2 * sizeof(int32_t), h->stream));
   GTD_CUDA(h, dp_launch_tree(p, h->stream));
-  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + 1024);
+  int32_t* h_io = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + kPinnedIo);
   GTD_CUDA(h, cudaMemcpyAsync(h_io, h->d_io, (kIoOrder + 64) * sizeof(int32_t), cudaMemcpyDeviceToHost,
                               h->stream));
   GTD_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -457,6 +483,41 @@ gtd_status gtd_dp_labels(gtd_handle h, const uint64_t* subsets, int count, int32
   GTD_CUDA(h, cudaMemcpyAsync(roots_out, d_roots, count * sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream));
   GTD_CUDA(h, cudaStreamSynchronize(h->stream));
   return GTD_OK;
+}
+
+gtd_status gtd_abort(gtd_handle h) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  // Only the abort stream and the pinned abort word are touched, so this may
+  // run while another host thread is inside a call on the same handle. The
+  // persistent kernels poll the error word and stop; the host loops see it.
+  DeviceGuard g(h->device);
+  int32_t* word = reinterpret_cast<int32_t*>(static_cast<char*>(h->h_pinned) + kPinnedAbort);
+  *word = kDevAborted;
+  cudaError_t e = cudaMemcpyAsync(h->d_io + kIoError, word, sizeof(int32_t), cudaMemcpyHostToDevice,
+                                  h->abort_stream);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(h->abort_stream);
+  return e == cudaSuccess ? GTD_OK : GTD_CUDA_ERROR;
+}
+
+gtd_status gtd_inject_fault(int kind, int count) {
+  if (count < 0)
+    return GTD_INVALID_ARG;
+  switch (kind) {
+    case GTD_FAULT_NONE:
+      g_alloc_faults.store(0);
+      g_stall_faults.store(0);
+      return GTD_OK;
+    case GTD_FAULT_ALLOC:
+      g_alloc_faults.store(count);
+      return GTD_OK;
+    case GTD_FAULT_STALL:
+      g_stall_faults.store(count);
+      return GTD_OK;
+    default:
+      return GTD_INVALID_ARG;
+  }
 }
 
 uint64_t gtd_dp_table_index(int n, int tile_bits, uint64_t subset_mask) {

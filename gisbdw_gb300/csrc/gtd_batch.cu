@@ -168,7 +168,12 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   st.tiles = static_cast<int>(P.total_tiles);
   st.ctas = static_cast<int>(ctas);
 
-  if (use_graph && h->bgraph_valid && h->bgraph_key == key) {
+  // The captured graph holds the handle's buffer addresses: replay only while
+  // no other call has reallocated them (a larger single solve grows the table).
+  const DpBatchParams& cap = h->bparams;
+  const bool same_buffers = cap.table == h->d_table && cap.flags == h->d_flags && cap.tile_map == h->d_tile_map &&
+                            cap.level_base == h->d_level_base && cap.graphs == h->d_bgraphs;
+  if (use_graph && h->bgraph_valid && h->bgraph_key == key && same_buffers) {
     st.graph_replayed = 1;
     GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
     GTD_CUDA(h, cudaGraphLaunch(h->bgraph, h->stream));
@@ -180,27 +185,13 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   // Device state for this shape.
   h->have_table = false;
   h->bgraph_valid = false;
-  void* p = h->d_table;
-  GTD_CUDA(h, ensure_device(&p, &h->table_cap, P.table_bytes));
-  h->d_table = static_cast<uint8_t*>(p);
+  GTD_CUDA(h, ensure_field(&h->d_table, &h->table_cap, P.table_bytes));
   gtd_status s = ensure_flags(h, P.total_tiles);
   if (s != GTD_OK)
     return s;
-  p = h->d_tile_map;
-  size_t cap = h->tile_map_cap * sizeof(uint2);
-  GTD_CUDA(h, ensure_device(&p, &cap, P.total_tiles * sizeof(uint2)));
-  h->d_tile_map = static_cast<uint2*>(p);
-  h->tile_map_cap = cap / sizeof(uint2);
-  p = h->d_level_base;
-  cap = h->level_base_cap * sizeof(uint32_t);
-  GTD_CUDA(h, ensure_device(&p, &cap, P.level_base.size() * sizeof(uint32_t)));
-  h->d_level_base = static_cast<uint32_t*>(p);
-  h->level_base_cap = cap / sizeof(uint32_t);
-  p = h->d_bgraphs;
-  cap = h->bgraphs_cap * sizeof(DpGraph);
-  GTD_CUDA(h, ensure_device(&p, &cap, count * sizeof(DpGraph)));
-  h->d_bgraphs = static_cast<DpGraph*>(p);
-  h->bgraphs_cap = cap / sizeof(DpGraph);
+  GTD_CUDA(h, ensure_field(&h->d_tile_map, &h->tile_map_cap, P.total_tiles));
+  GTD_CUDA(h, ensure_field(&h->d_level_base, &h->level_base_cap, P.level_base.size()));
+  GTD_CUDA(h, ensure_field(&h->d_bgraphs, &h->bgraphs_cap, size_t(count)));
   // Descriptors and level bases go up through pinned staging (synchronised
   // below, so the staging is released right after).
   const size_t gbytes = count * sizeof(DpGraph), lbytes = P.level_base.size() * sizeof(uint32_t);
@@ -373,21 +364,9 @@ gtd_status gtd_dp_solve_batch(gtd_handle h, const gtd_graph_desc* descs, int cou
   s = grow_pinned(h, adj_bytes + out_bytes);
   if (s != GTD_OK)
     return s;
-  void* p = h->d_badj;
-  size_t cap = h->badj_cap * sizeof(uint64_t);
-  GTD_CUDA(h, ensure_device(&p, &cap, adj_bytes));
-  h->d_badj = static_cast<uint64_t*>(p);
-  h->badj_cap = cap / sizeof(uint64_t);
-  p = h->d_btd;
-  cap = h->btd_cap * sizeof(int32_t);
-  GTD_CUDA(h, ensure_device(&p, &cap, count * sizeof(int32_t)));
-  h->d_btd = static_cast<int32_t*>(p);
-  h->btd_cap = cap / sizeof(int32_t);
-  p = h->d_bparent;
-  cap = h->bparent_cap * sizeof(int32_t);
-  GTD_CUDA(h, ensure_device(&p, &cap, size_t(pool_len) * sizeof(int32_t)));
-  h->d_bparent = static_cast<int32_t*>(p);
-  h->bparent_cap = cap / sizeof(int32_t);
+  GTD_CUDA(h, ensure_field(&h->d_badj, &h->badj_cap, size_t(pool_len)));
+  GTD_CUDA(h, ensure_field(&h->d_btd, &h->btd_cap, size_t(count)));
+  GTD_CUDA(h, ensure_field(&h->d_bparent, &h->bparent_cap, size_t(pool_len)));
 
   char* stage = static_cast<char*>(h->h_bstage);
   std::memcpy(stage, adj_pool, adj_bytes);

@@ -334,6 +334,7 @@ struct StopCheck {
   const uint32_t* exited = nullptr; // warps that left this pass, items started in it:
   uint32_t drain_at = 0;            // a pass that started at least one item per warp
   uint32_t full_at = 0;             // drains once half of its warps have left
+  const int32_t* error = nullptr;   // the launch's error word: an abort or an error elsewhere
 };
 
 struct Search {
@@ -736,7 +737,8 @@ struct Search {
                                 ld_acquire_u32(stop.exited + 1) >= stop.full_at)))
         flag = 3;  // budget spent, or the pass is draining: back next pass with twice the budget
       else if ((stop.best && static_cast<int>(ld_acquire_u32(stop.best) >> 8) <= stop.item_k) ||
-               (stop.lbp && static_cast<int>(ld_acquire_u32(stop.lbp)) > stop.item_k))
+               (stop.lbp && static_cast<int>(ld_acquire_u32(stop.lbp)) > stop.item_k) ||
+               (stop.error && ld_relaxed_s32(stop.error) != 0))
         flag = 2;
     }
     flag = __shfl_sync(0xffffffffu, flag, 0);
@@ -1113,6 +1115,7 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 6) bnb_kernel(const __grid_con
     s.stop.exited = p.exited;
     s.stop.drain_at = p.drain_at;
     s.stop.full_at = p.full_at;
+    s.stop.error = p.error;
     if (lane == 0 && p.exited)
       atomicAdd(p.exited + 1, 1u);
     if (p.deadline_ns) {
@@ -1313,11 +1316,7 @@ int mmd_host(const uint64_t* adj2, int n) {
 
 template <typename T>
 gtd_status grow(gtd_handle h, T** p, size_t* cap, size_t count) {
-  void* q = *p;
-  size_t bytes = *cap * sizeof(T);
-  GTD_CUDA(h, ensure_device(&q, &bytes, count * sizeof(T)));
-  *p = static_cast<T*>(q);
-  *cap = bytes / sizeof(T);
+  GTD_CUDA(h, ensure_field(p, cap, count));
   return GTD_OK;
 }
 

@@ -21,6 +21,9 @@ constexpr int kIoTd = 4;
 constexpr int kIoParent = 8;
 constexpr int kIoOrder = 72;
 constexpr int kIoWords = 256;
+// Byte offsets inside the handle's 4096-byte pinned staging block.
+constexpr size_t kPinnedIo = 1024;     // IO block copies (kIoOrder + 64 words)
+constexpr size_t kPinnedAbort = 4092;  // gtd_abort's source word
 
 // Flag stamp reserved for CUDA-graph replays (the graph zeroes the flags
 // first); direct launches cycle their epochs through [1, kGraphEpoch).
@@ -48,7 +51,8 @@ struct gtd_handle_s {
   uint32_t epoch = 0;
   int32_t* d_io = nullptr;   // control/IO block
   uint64_t* d_adj = nullptr; // kDpMaxN masks
-  void* h_pinned = nullptr;  // staging for adj (in) and the IO block (out)
+  void* h_pinned = nullptr;  // staging for adj (in) and the IO block (out); word kPinnedAbort: abort code
+  cudaStream_t abort_stream = nullptr;  // gtd_abort's copy of the abort code (non-blocking)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
   // Batched DP buffers.
@@ -91,8 +95,28 @@ gtd_status fail(gtd_handle h, gtd_status s, const std::string& msg);
 gtd_status cuda_fail(gtd_handle h, cudaError_t e, const char* what);
 gtd_status check_adjacency(gtd_handle h, const uint64_t* adj, int n);
 gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info);
-// Grows a device buffer to at least `bytes` (contents not kept).
+// Grows a device buffer to at least `bytes` (contents not kept). On failure
+// *ptr is null and *cap 0 (the old buffer is already freed).
 cudaError_t ensure_device(void** ptr, size_t* cap, size_t bytes);
+
+// ensure_device on a typed field of the handle, capacity in elements: the
+// field is updated whether or not the allocation succeeds, so it never keeps
+// a freed pointer.
+template <typename T>
+cudaError_t ensure_field(T** field, size_t* cap_elems, size_t count) {
+  void* q = *field;
+  size_t bytes = *cap_elems * sizeof(T);
+  const cudaError_t e = ensure_device(&q, &bytes, count * sizeof(T));
+  *field = static_cast<T*>(q);
+  *cap_elems = bytes / sizeof(T);
+  return e;
+}
+
+// Test fault injection (gtd_inject_fault), process-wide: consumes one
+// pending device-allocation failure (true: fail this allocation) or one
+// pending DP stall (true: the launch skips its first tile).
+bool take_alloc_fault();
+bool take_stall_fault();
 // Grows the flag array; fresh flags are zeroed and the epoch restarts.
 gtd_status ensure_flags(gtd_handle h, size_t tiles);
 // Next epoch for a direct (non-graph) launch.

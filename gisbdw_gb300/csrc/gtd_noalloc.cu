@@ -15,34 +15,39 @@
 // rejected with GTD_INVALID_ARG.
 //
 // The array's name is only a host-side stand-in for the device symbol, so
-// host code never passes it to a kernel: on the first call on each device,
-// with that device current, the address is looked up once with
-// cudaGetSymbolAddress and cached. That first call should therefore happen
-// before any stream capture begins on the device.
+// host code never passes it to a kernel: every call, with the caller's device
+// current, looks the address up with cudaGetSymbolAddress (cheap once the
+// module is loaded) and checks the result, so a context that was reset and
+// made again (which reloads the module at a new address) is never written
+// through a stale pointer. The first call on a device loads the module, so
+// it should happen before any stream capture begins on that device.
 //
 // Every call shares the one array, which keeps what the previous call left:
 // the work counter and error word are cleared on each call, and tile flags
 // carry a per-device epoch that increases with every call (the flags are
-// cleared when it wraps). Calls whose GPU work overlaps — on two streams, or
-// from two host threads — race on the array and give undefined results.
+// cleared when it wraps, gtd_noalloc_epoch.h). Calls whose GPU work
+// overlaps — on two streams, or from two host threads — race on the array
+// and give undefined results.
 #include <cuda_runtime.h>
 
-#include <atomic>
 #include <cstdint>
 #include <mutex>
 
 #include "../../include/gtd.h"
 #include "gtd_device.cuh"
 #include "gtd_dp_kernels.h"
+#include "gtd_noalloc_epoch.h"
 
 namespace gtd {
 namespace {
 
 constexpr int kNoallocTileBits = 10;
 constexpr size_t kNoallocTableBytes = size_t(1) << GTD_DP_NOALLOC_MAX_N;
-// Tiles of the largest accepted graph at the smallest tile size the layout
-// can choose (n = 24 keeps lb = 10 unless n < 10; 2^14 tiles).
-constexpr size_t kNoallocMaxTiles = size_t(1) << (GTD_DP_NOALLOC_MAX_N - 8);
+// Tiles of the largest accepted graph: make_dp_layout(n, 10) keeps 10 tile
+// bits for 10 <= n <= 24 (2^(n - 10) tiles) and one tile below that.
+constexpr size_t kNoallocMaxTiles = size_t(1) << (GTD_DP_NOALLOC_MAX_N - kNoallocTileBits);
+static_assert(kNoallocTileBits >= kDpMinTileBits && kNoallocTileBits <= kDpMaxTileBits,
+              "make_dp_layout must keep the fixed tile size");
 constexpr size_t kNoallocFlagsOffset = kNoallocTableBytes;
 constexpr size_t kNoallocCtrlOffset = kNoallocFlagsOffset + kNoallocMaxTiles * sizeof(uint32_t);
 constexpr size_t kNoallocScratchBytes = kNoallocCtrlOffset + 256;
@@ -51,33 +56,8 @@ constexpr size_t kNoallocScratchBytes = kNoallocCtrlOffset + 256;
 __device__ __align__(256) uint8_t g_noalloc_scratch[kNoallocScratchBytes];
 
 constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-uint8_t* g_scratch_ptr[kMaxDevices] = {};
-int g_num_sms[kMaxDevices] = {};
-std::atomic<uint32_t> g_epoch[kMaxDevices];
-
-// Once per device, with that device current: resolve the array's device
-// address. Returns nullptr (and the CUDA error in *err) on failure.
-uint8_t* scratch_for_device(int dev, cudaError_t* err) {
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_scratch_ptr[dev])
-    return g_scratch_ptr[dev];
-  void* ptr = nullptr;
-  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-  if (e != cudaSuccess) {
-    *err = e;
-    return nullptr;
-  }
-  int sms = 0;
-  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) {
-    *err = e;
-    return nullptr;
-  }
-  g_num_sms[dev] = sms;
-  g_scratch_ptr[dev] = static_cast<uint8_t*>(ptr);
-  return g_scratch_ptr[dev];
-}
+std::mutex g_epoch_mutex;
+uint32_t g_epoch[kMaxDevices] = {};
 
 gtd_status map_error(int32_t code) {
   switch (code) {
@@ -101,9 +81,13 @@ extern "C" gtd_status gtd_dp_solve_noalloc(const uint64_t* d_adj, int n, int32_t
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return GTD_CUDA_ERROR;
-  cudaError_t err = cudaSuccess;
-  uint8_t* base = scratch_for_device(dev, &err);
-  if (!base)
+  // The scratch's address in the current context (see the top of the file).
+  void* sym = nullptr;
+  if (cudaGetSymbolAddress(&sym, g_noalloc_scratch) != cudaSuccess || !sym)
+    return GTD_CUDA_ERROR;
+  uint8_t* const base = static_cast<uint8_t*>(sym);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
     return GTD_CUDA_ERROR;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
@@ -128,20 +112,19 @@ extern "C" gtd_status gtd_dp_solve_noalloc(const uint64_t* d_adj, int n, int32_t
   p.td_out = d_td;
   p.parent_out = d_parent;
   p.order_out = d_order;
-  uint32_t epoch = g_epoch[dev].fetch_add(1) + 1;
-  if (epoch == 0 || epoch == 0xffffffffu) {
-    // wrapped: clear every flag so that no stale stamp matches
-    if (cudaMemsetAsync(p.flags, 0, kNoallocMaxTiles * sizeof(uint32_t), s) != cudaSuccess)
-      return GTD_CUDA_ERROR;
-    g_epoch[dev].store(1);
-    epoch = 1;
+  bool clear_flags = false;
+  {
+    std::lock_guard<std::mutex> lock(g_epoch_mutex);
+    g_epoch[dev] = noalloc_next_epoch(g_epoch[dev], &clear_flags);
+    p.epoch = g_epoch[dev];
   }
-  p.epoch = epoch;
+  if (clear_flags && cudaMemsetAsync(p.flags, 0, kNoallocMaxTiles * sizeof(uint32_t), s) != cudaSuccess)
+    return GTD_CUDA_ERROR;  // wrapped: no stale stamp may match the new epoch
 
   int occ = dp_tile_occupancy(p.lb);
   if (occ < 1)
     occ = 1;
-  long long ctas = static_cast<long long>(g_num_sms[dev]) * occ;
+  long long ctas = static_cast<long long>(sms) * occ;
   if (ctas > p.total_tiles)
     ctas = p.total_tiles;
   if (cudaMemsetAsync(ctrl, 0, 4 * sizeof(int32_t), s) != cudaSuccess)

@@ -24,6 +24,10 @@ from . import _lib
 from .graphs import Graph
 
 
+# Treedepth of a Result when a solve gave none (the reference's UINT_MAX).
+NO_RESULT = 2**32 - 1
+
+
 @dataclass
 class Result:
     """``EliminationTree::Result`` (elimination_tree.hpp:26-30): the tree as
@@ -70,9 +74,20 @@ class DynamicGPU:
         self.stats: dict = {}
 
     def __call__(self, g: Graph) -> None:
+        """Solves g. Running out of device memory is swallowed as the
+        reference's DP functors swallow std::bad_alloc (dynamic_cpu.hpp:52-56):
+        the solver then holds no result, :meth:`Result` gives treedepth
+        NO_RESULT (UINT_MAX, dynamic_cpu.hpp:79-80) and GetElimination []."""
         if g.n > _lib.DP_MAX_N:
             raise _lib.InvalidArgument(1, f"subset DP supports n <= {_lib.DP_MAX_N}")
-        td, parent, order, stats = self._h.dp_solve(_masks(g), g.n, tile_bits=self._tile_bits)
+        self._n, self._td, self._parent, self._order = g.n, None, None, None
+        try:
+            td, parent, order, stats = self._h.dp_solve(_masks(g), g.n, tile_bits=self._tile_bits)
+        except _lib.GtdError as e:
+            if e.status == 3:  # GTD_OOM
+                self._td = NO_RESULT
+                return
+            raise
         self._n, self._td, self._parent, self._order, self.stats = g.n, td, parent, order, stats
 
     @property
@@ -84,6 +99,8 @@ class DynamicGPU:
     def Result(self) -> Result:
         if self._td is None:
             raise _lib.GtdError(7, "no solve yet")
+        if self._td == NO_RESULT:
+            return Result(NO_RESULT, -1, np.zeros(0, dtype=np.int32))
         roots = np.flatnonzero(self._parent == -1)
         return Result(self._td, int(roots[0]) if len(roots) else -1, self._parent.copy())
 
@@ -91,6 +108,8 @@ class DynamicGPU:
         """Elimination order of the subset of rank ``subset_code`` among the
         ``subset_size``-subsets of ``nverts`` vertices (dynamic_gpu.hpp:48-64).
         The full vertex set is (n, n, 0)."""
+        if self._td == NO_RESULT:
+            return []
         if subset_size == nverts == self._n and subset_code == 0 and self._order is not None:
             return self._order.tolist()
         td, order = self._h.dp_query(_decode(nverts, subset_size, subset_code))
@@ -106,7 +125,11 @@ class BnBGPU:
     (``td::BnBGPU``, bnb_gpu.hpp:12-17: ``solver(g, heur_td) -> int``).
     Unlike the reference it also returns the elimination tree
     (:meth:`Result`). ``order`` is the branching order (vertex tried first
-    at rank 0); by default ascending ids, the reference's DefaultAttemptOrder."""
+    at rank 0); by default ascending ids, the reference's DefaultAttemptOrder.
+    ``heur_td`` below the seed tree's height is honoured as the reference's
+    initial best_td (bnb_gpu.cu:275): the search decides level heur_td - 1
+    first and, if that fails, heur_td (which yields the tree); it only orders
+    the search, so a wrong bound cannot change the result."""
 
     def __init__(self, device: int = 0, handle: Optional[_lib.Handle] = None, deadline_ns: int = 0):
         self._h = handle or _lib.Handle(device)
@@ -116,10 +139,11 @@ class BnBGPU:
     def __call__(self, g: Graph, heur_td: Optional[int] = None, order=None, seed=None) -> int:
         if seed is None:
             seed = _lib.heuristic(g, 0)
-        if heur_td is not None and heur_td < seed[0]:
-            raise _lib.InvalidArgument(1, "heur_td below the seed tree's height needs its tree (pass seed=)")
+        hints = None
+        if heur_td is not None and 2 <= heur_td < seed[0]:
+            hints = np.array([heur_td - 1], dtype=np.int32)
         res = self._h.bnb_solve_batch([g], orders=[order] if order is not None else None, seeds=[seed],
-                                      deadline_ns=self._deadline)
+                                      deadline_ns=self._deadline, hints=hints)
         self._res = res
         return int(res["td"][0])
 

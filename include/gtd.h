@@ -49,6 +49,29 @@ const char* gtd_status_string(gtd_status s);
 /* Human-readable detail of the last failure on this handle. */
 const char* gtd_last_error(gtd_handle h);
 
+/* Stops the call in flight on handle h: the persistent kernels see the
+ * request at their next poll (every DP tile ticket and dependency wait,
+ * every 64 branch-and-bound search nodes) and that call returns GTD_ABORTED
+ * with its outputs undefined; the handle stays usable. This is the one call
+ * that may be made from another host thread while a call on the same handle
+ * runs. A request made while no call runs is dropped when the next call
+ * starts (every call clears the handle's error word first). No counterpart
+ * in the reference, whose solvers run to completion. */
+gtd_status gtd_abort(gtd_handle h);
+
+/* Fault injection for tests of the error paths (no counterpart in the
+ * reference), process-wide:
+ *   GTD_FAULT_ALLOC, c: the c-th device buffer allocation made by this
+ *     library from now on fails as if the GPU were out of memory; the call
+ *     returns GTD_OOM and the handle stays usable;
+ *   GTD_FAULT_STALL, c: the next c single-graph DP solves (gtd_dp_solve,
+ *     gtd_dp_solve_device) never take their first tile, so every tile that
+ *     depends on it waits until its bound (gtd_dp_opts.timeout_ns) runs out:
+ *     GTD_TIMEOUT, and the handle stays usable;
+ *   GTD_FAULT_NONE: clears both. */
+enum { GTD_FAULT_NONE = 0, GTD_FAULT_ALLOC = 1, GTD_FAULT_STALL = 2 };
+gtd_status gtd_inject_fault(int kind, int count);
+
 /* Options and statistics of one subset-DP solve. */
 typedef struct {
   int tile_bits;        /* low vertices per tile (0 = autotuned default) */

@@ -20,9 +20,15 @@
 //   GTD_INVALID_ARG, GTD_NOT_CONNECTED -> std::invalid_argument
 //   GTD_OOM                           -> std::bad_alloc
 //   anything else                     -> std::runtime_error
+// except that td::DynamicGPU swallows running out of device memory the way
+// the reference's DP functors swallow std::bad_alloc (dynamic_cpu.hpp:52-56,
+// dynamic_cpu_improv.hpp:58-72): the call returns with no result,
+// GetElimination then gives an empty list and Decompose() the reference's
+// "no result" sentinel, treedepth = UINT_MAX (dynamic_cpu.hpp:79-80).
 #pragma once
 
 #include <cstdint>
+#include <limits>
 #include <list>
 #include <new>
 #include <stdexcept>
@@ -122,17 +128,26 @@ class DynamicGPU {
     parent_.assign(n_, -1);
     order_.assign(n_, 0);
     int32_t td = 0;
-    gtd::check(gtd_dp_solve(handle_.get(), adj_.data(), n_, &td, parent_.data(), order_.data(), nullptr,
-                            &stats_),
-               handle_.get());
+    have_ = false;
+    const gtd_status s = gtd_dp_solve(handle_.get(), adj_.data(), n_, &td, parent_.data(), order_.data(),
+                                      nullptr, &stats_);
+    if (s == GTD_OOM) {  // the reference's catch (std::bad_alloc const&) { return; }
+      parent_.clear();
+      order_.clear();
+      return;
+    }
+    gtd::check(s, handle_.get());
     td_ = td;
+    have_ = true;
   }
 
   // Elimination order of the subset with colex rank subset_code among the
   // subset_size-subsets of nverts vertices (dynamic_gpu.hpp:48-64);
-  // (n, n, 0) is the whole graph.
+  // (n, n, 0) is the whole graph. Empty when the last call gave no result.
   template <typename VertexType>
   std::list<VertexType> GetElimination(std::size_t nverts, std::size_t subset_size, std::size_t subset_code) {
+    if (!have_)
+      return {};
     if (nverts == static_cast<std::size_t>(n_) && subset_size == nverts && subset_code == 0)
       return std::list<VertexType>(order_.begin(), order_.end());
     uint64_t mask = Decode(nverts, subset_size, subset_code);
@@ -143,9 +158,14 @@ class DynamicGPU {
   }
 
   // The tree the reference's main builds from GetElimination
-  // (main.cpp:187-195): parent array, height and root.
+  // (main.cpp:187-195): parent array, height and root; with no result, an
+  // empty tree of height UINT_MAX (the reference's sentinel).
   gtd::Result Decompose() const {
     gtd::Result r;
+    if (!have_) {
+      r.treedepth = std::numeric_limits<unsigned>::max();
+      return r;
+    }
     r.parent = parent_;
     r.treedepth = static_cast<unsigned>(td_);
     for (int v = 0; v < n_; ++v)
@@ -156,7 +176,8 @@ class DynamicGPU {
     return r;
   }
 
-  unsigned Treedepth() const { return static_cast<unsigned>(td_); }
+  unsigned Treedepth() const { return have_ ? static_cast<unsigned>(td_) : std::numeric_limits<unsigned>::max(); }
+  bool HasResult() const { return have_; }
   const gtd_dp_stats& Stats() const { return stats_; }
 
  private:
@@ -188,16 +209,24 @@ class DynamicGPU {
   std::vector<int32_t> parent_, order_;
   int n_ = 0;
   int td_ = 0;
+  bool have_ = false;
   gtd_dp_stats stats_{};
 };
 
 // Exact treedepth by the GB300 branch and bound (persistent kernel), the
 // call shape of BnBGPU (bnb_gpu.hpp:12-17): operator()(g, heur_td) returns
-// the treedepth. The incumbent is the better of the library's reference
-// heuristic chain (HighestDegree(Variance), gtd_heuristic kind 0) and
-// heur_td when it does not exceed that chain's value; unlike the reference,
-// the result also carries a tree (Decompose). A disconnected graph throws
-// std::invalid_argument, as BranchAndBound does (branch_and_bound.hpp:67-75).
+// the treedepth. The incumbent tree comes from the library's reference
+// heuristic chain (HighestDegree(Variance), gtd_heuristic kind 0). A caller's
+// heur_td below that chain's height is honoured as the reference's initial
+// best_td (bnb_gpu.cu:275) is: the search starts at level heur_td - 1, and if
+// no tree of that height exists it decides level heur_td next, which also
+// yields the tree (a bound without a tree cannot be returned as one). The
+// bound only orders the search, so a wrong heur_td cannot change the result.
+// n <= GTD_BNB_MAX_N (104; the reference's BnBGPU takes n <= 127, int8
+// vertices, bnb_gpu.cu:107-165, and BranchAndBound n <= 128): larger graphs
+// throw std::invalid_argument. Unlike the reference, the result also carries
+// a tree (Decompose). A disconnected graph throws std::invalid_argument, as
+// BranchAndBound does (branch_and_bound.hpp:67-75).
 class BnBGPU {
  public:
   explicit BnBGPU(int device = 0, uint64_t deadline_ns = 0) : handle_(device), deadline_ns_(deadline_ns) {}
@@ -211,13 +240,14 @@ class BnBGPU {
     std::vector<int32_t> seed_parent(n);
     int32_t seed_td = 0;
     gtd::check(gtd_heuristic(adj.data(), n, 0, nullptr, &seed_td, seed_parent.data()), handle_.get());
-    (void)heur_td;  // a bound without a tree cannot seed: the chain's tree does
+    // heur_td < seed: decide level heur_td - 1 first (then heur_td if that fails)
+    int32_t hint = (heur_td >= 2 && static_cast<int32_t>(heur_td) < seed_td) ? static_cast<int32_t>(heur_td) - 1 : 0;
     gtd_graph_desc desc{n, 0};
     int32_t td = 0, status = 0;
     float proof_ms = 0;
     uint64_t nodes = 0;
     parent_.assign(n, -1);
-    gtd_bnb_opts opts{0, deadline_ns_, 0, nullptr, 0, 0};
+    gtd_bnb_opts opts{0, deadline_ns_, 0, hint > 0 ? &hint : nullptr, 0, 0};
     gtd::check(gtd_bnb_solve_batch(handle_.get(), &desc, 1, adj.data(), n, nullptr, &seed_td, seed_parent.data(),
                                    &td, parent_.data(), &status, &proof_ms, &nodes, &opts, &stats_),
                handle_.get());

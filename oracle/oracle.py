@@ -23,7 +23,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libgtd_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libgtdref.so")
-REF_SRC = os.environ.get("GTD_REFERENCE_TREEDEPTH", "/root/reference/Treedepth")
+# The reference's Treedepth/ sources: $GTD_REFERENCE_TREEDEPTH, else a
+# checkout named `reference` beside this repository.
+REF_SRC = os.environ.get("GTD_REFERENCE_TREEDEPTH",
+                         os.path.normpath(os.path.join(HERE, "..", "..", "reference", "Treedepth")))
 
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -84,7 +87,7 @@ class Port:
 
     def dp_table(self, g, nthreads: int = 1) -> np.ndarray:
         adj = g.adj64()
-        T = np.zeros(1 << g.n, dtype=np.uint8)
+        T = np.empty(1 << g.n, dtype=np.uint8)  # gtdo_dp_table writes every entry
         rc = self.L.gtdo_dp_table(g.n, _ptr(adj), _ptr(T), nthreads)
         if rc:
             raise ValueError(f"gtdo_dp_table rc={rc}")

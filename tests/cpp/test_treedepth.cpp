@@ -57,5 +57,19 @@ int main() {
   } catch (std::invalid_argument const&) {
     std::printf("invalid_argument\n");
   }
+  // a caller's bound only orders the search: a correct one (3 for P7) and a
+  // wrong one (3 for C5, whose treedepth is 4) give the exact treedepth
+  std::printf("heur %d %d\n", bnb(p7, 3), bnb(c5, 3));
+  // out of device memory: no result and the reference's sentinel
+  // (dynamic_cpu.hpp:52-56, 79-80), then the next call succeeds
+  Graph p20(20);
+  for (int i = 0; i < 19; ++i)
+    boost::add_edge(i, i + 1, p20);
+  gtd_inject_fault(GTD_FAULT_ALLOC, 1);
+  dyngpu(p20);
+  std::printf("oom %d %u %zu\n", dyngpu.HasResult() ? 1 : 0, dyngpu.Decompose().treedepth,
+              dyngpu.GetElimination<std::size_t>(20, 20, 0).size());
+  dyngpu(p20);
+  std::printf("after %d %u\n", dyngpu.HasResult() ? 1 : 0, dyngpu.Decompose().treedepth);
   return 0;
 }

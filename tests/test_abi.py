@@ -86,3 +86,40 @@ def test_batch_parents_are_per_graph_views():
     assert [x.tolist() for x in pg[1::2]] == [x.tolist() for x in want[1::2]]
     assert np.shares_memory(pg[0], flat)
     assert len(_lib.PerGraph(flat, (_lib.GraphDesc * 0)())) == 0
+
+
+def test_noalloc_source_allocates_nothing():
+    """The no-allocation entry point's translation unit calls no allocator."""
+    src = open(os.path.join(ROOT, "gisbdw_gb300", "csrc", "gtd_noalloc.cu")).read()
+    code = re.sub(r"//[^\n]*", "", re.sub(r"/\*.*?\*/", "", src, flags=re.S))
+    for name in ("cudaMalloc", "cudaFree", "cudaMallocAsync", "cudaMallocManaged", "cudaHostAlloc", "malloc(",
+                 "new "):
+        assert name not in code, name
+
+
+def test_noalloc_epoch_wraps_and_clears(tmp_path):
+    """The shared flags' epoch: first call clears, then 2, 3, ...; after the
+    last epoch the next call is 1 again and clears every flag."""
+    import subprocess
+    prog = tmp_path / "epoch.cpp"
+    prog.write_text("""
+#include <cstdio>
+#include "gtd_noalloc_epoch.h"
+int main() {
+  bool c = false;
+  unsigned e = gtd::noalloc_next_epoch(0, &c);
+  std::printf("%u %d\\n", e, (int)c);
+  e = gtd::noalloc_next_epoch(e, &c);
+  std::printf("%u %d\\n", e, (int)c);
+  e = gtd::noalloc_next_epoch(gtd::kNoallocLastEpoch - 1, &c);
+  std::printf("%u %d\\n", e, (int)c);
+  e = gtd::noalloc_next_epoch(e, &c);
+  std::printf("%u %d\\n", e, (int)c);
+  return 0;
+}
+""")
+    exe = str(tmp_path / "epoch")
+    subprocess.run(["g++", "-std=c++17", "-I" + os.path.join(ROOT, "gisbdw_gb300", "csrc"), str(prog), "-o", exe],
+                   check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    assert out == ["1", "1", "2", "0", str(0xFFFFFFFE), "0", "1", "1"]

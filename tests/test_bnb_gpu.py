@@ -67,6 +67,37 @@ def test_bnb_equals_dp_sparse_n28_to_32(handle):
         assert t == handle.dp_solve(g.adj64(), g.n)[0], g.name
 
 
+def _family_graphs_33_to_36():
+    """Connected graphs of the sparse B&B families with n in [33, 36], where
+    the subset DP still answers exactly (tables of 8-64 GiB)."""
+    gs = []
+    for i, n in enumerate((33, 34, 35, 36)):
+        gs.append(G.random_geometric(n, 3.0 + 0.6 * i, 700 + n))
+        gs.append(G.grid_deleted(n, 0.1, 700 + n))
+        gs.append(G.tree_plus_edges(n, n // 4, 700 + n))
+    gs += [G.random_regular3(n, s) for n in (34, 36) for s in (1, 2)]
+    return gs
+
+
+def test_bnb_equals_dp_n33_to_36(handle):
+    """K2 against K1 above n = 32 on the config-4/5 families: every graph the
+    branch and bound proves within the cap has the DP's treedepth."""
+    gs = _family_graphs_33_to_36()
+    res = handle.bnb_solve_batch(gs, deadline_ns=60 * 10**9)
+    proven = res["status"] == 0
+    for g, t, par in zip(gs, res["td"], res["parents"]):
+        assert check_tree(g, int(t), par), g.name
+    # random geometric, deleted grids and trees plus edges are proven well inside the cap
+    assert all(p for g, p in zip(gs, proven) if not g.name.startswith("reg3")), \
+        [g.name for g, p in zip(gs, proven) if not p]
+    checked = 0
+    for g, t, ok in zip(gs, res["td"], proven):
+        if ok:
+            assert int(t) == handle.dp_solve(g.adj64(), g.n, want_order=False)[0], g.name
+            checked += 1
+    assert checked >= 12
+
+
 def test_bnb_class_layer(handle):
     g = G.gnp_connected(16, 0.3, 2)
     b = BnBGPU(handle=handle)
@@ -74,6 +105,12 @@ def test_bnb_class_layer(handle):
     r = b.Result()
     assert td == handle.dp_solve(g.adj64(), g.n)[0]
     assert check_tree(g, td, r.parent) and r.parent[r.root] == -1
+    # the reference's heur_td (bnb_gpu.hpp:12-17): a bound at, below (wrong)
+    # or above the treedepth only orders the search
+    for heur in (td, td - 1, td + 2, 2):
+        assert b(g, heur_td=heur) == td
+        r = b.Result()
+        assert check_tree(g, td, r.parent)
 
 
 def test_bnb_invalid_inputs(handle):
@@ -87,9 +124,12 @@ def test_bnb_invalid_inputs(handle):
 
 
 def test_bnb_deadline_reports_timeout_and_stays_usable(handle):
-    gs = G.config4_graphs(count=3)
+    gs = G.config4_graphs(count=3)  # a random geometric, a random 3-regular, a deleted grid
     res = handle.bnb_solve_batch(gs, deadline_ns=1000)
     assert set(res["status"].tolist()) <= {0, 4}
+    # the 3-regular graph (n >= 40) cannot be proven in a microsecond: its
+    # deadline must run out and be reported
+    assert gs[1].name.startswith("reg3") and res["status"][1] == 4
     for g, t, par in zip(gs, res["td"], res["parents"]):
         assert check_tree(g, t, par)  # best found so far is still a valid tree
     r2 = _check(handle, [G.cycle(9)])

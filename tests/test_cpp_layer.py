@@ -43,3 +43,6 @@ def test_cpp_layer_matches_oracle(tmp_path, port):
         tag, t, td, root = line.split()
         assert tag == "bnb" and int(t) == want and int(td) == want
     assert out[5] == "invalid_argument"
+    assert out[6] == "heur 3 4"
+    assert out[7] == f"oom 0 {2**32 - 1} 0"  # no result, UINT_MAX sentinel, empty order
+    assert out[8] == "after 1 5"  # td(P20) = ceil(log2(21))

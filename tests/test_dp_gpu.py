@@ -104,6 +104,22 @@ def test_dp_larger_graphs_match_oracle(handle, port):
         assert td == otd and parent.tolist() == opar.tolist(), g.name
 
 
+@pytest.mark.slow
+@pytest.mark.parametrize("idx", range(9))
+def test_dp_config2_bit_exact(handle, port, idx):
+    """The headline workload's graphs (n = 28, 30, 32 and the 5 x 6 grid):
+    treedepth, parent array and GetElimination order bit-exact against the
+    oracle's restatement of DynamicGPU (multi-threaded on the host)."""
+    import os
+    g = G.config2_graphs()[idx]
+    td, parent, order, _ = handle.dp_solve(g.adj64(), g.n)
+    T = port.dp_table(g, nthreads=os.cpu_count() or 8)
+    otd, opar = port.tree_from_table(g, T)
+    assert td == otd, g.name
+    assert parent.tolist() == opar.tolist(), g.name
+    assert order.tolist() == port.get_elimination(g, T, _full(g.n)), g.name
+
+
 def test_dp_config2_sized_properties(handle, port):
     """n = 30: no oracle table in seconds; check size-independent facts:
     the tree is valid with height = td, the elimination order replays to the
@@ -202,13 +218,36 @@ def test_dp_invalid_inputs(handle):
     assert handle.dp_solve(adj, 5)[0] == 3
 
 
-def test_dp_short_wait_limit_keeps_context_usable(handle):
-    """A 1 ns bound on every dependency wait: the solve either finishes or
-    reports GTD_TIMEOUT; either way no hang, and the next solve succeeds."""
+def test_dp_wait_bound_runs_out_and_context_stays_usable(handle, port):
+    """A dependency wait that can never be satisfied (the injected stall:
+    the level-0 tile is never computed) must end at its bound with
+    GTD_TIMEOUT, and the next solve on the same handle must be exact."""
     g = G.gnp_connected(24, 0.2, 3)
+    _lib.inject_fault(_lib.FAULT_STALL, 1)
     try:
-        handle.dp_solve(g.adj64(), g.n, timeout_ns=1)
-    except _lib.DeadlineExceeded:
-        pass
+        with pytest.raises(_lib.DeadlineExceeded):
+            handle.dp_solve(g.adj64(), g.n, timeout_ns=200_000_000)
+    finally:
+        _lib.inject_fault(_lib.FAULT_NONE, 0)
     td, parent, _, _ = handle.dp_solve(g.adj64(), g.n)
-    assert td > 0
+    otd, opar = port.dp_solve(g, nthreads=8)
+    assert td == otd and parent.tolist() == opar.tolist()
+
+
+def test_dp_device_path_reports_timeout_at_sync(handle):
+    """The asynchronous entry point reports the same timeout at gtd_sync."""
+    import torch
+    g = G.gnp_connected(22, 0.25, 4)
+    d_adj = torch.from_numpy(g.adj64().view(np.int64)).cuda()
+    d_out = torch.zeros(2 + 2 * g.n, dtype=torch.int32, device="cuda")
+    _lib.inject_fault(_lib.FAULT_STALL, 1)
+    try:
+        handle.dp_solve_device(d_adj.data_ptr(), g.n, d_out.data_ptr(), d_out[2:].data_ptr(),
+                               timeout_ns=200_000_000)
+        with pytest.raises(_lib.DeadlineExceeded):
+            handle.sync()
+    finally:
+        _lib.inject_fault(_lib.FAULT_NONE, 0)
+    handle.dp_solve_device(d_adj.data_ptr(), g.n, d_out.data_ptr(), d_out[2:].data_ptr())
+    handle.sync()
+    assert int(d_out[0].item()) == handle.dp_solve(g.adj64(), g.n)[0]

@@ -53,3 +53,43 @@ def test_noalloc_matches_allocating_entry_point():
     st = _noalloc(L, d_adj.data_ptr(), 25, d_buf.data_ptr(), d_buf.data_ptr(), 0, stream.cuda_stream)
     assert st == 1  # GTD_INVALID_ARG
     h.close()
+
+
+def test_noalloc_allocates_nothing_and_reports_bad_input():
+    """Across repeated calls the device's free memory and torch's allocation
+    stay the same; an asymmetric adjacency is rejected on the device
+    (GTD_INVALID_ARG, no hang); d_order may be NULL."""
+    import torch
+
+    from gisbdw_gb300 import Handle, _lib
+    from gisbdw_gb300 import graphs as G
+
+    L = _lib.load()
+    L.gtd_dp_solve_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    stream = torch.cuda.Stream()
+    g = G.gnp_connected(23, 0.2, 5)
+    d_adj = torch.from_numpy(g.adj64().view(np.int64)).cuda()
+    d_td = torch.zeros(1, dtype=torch.int32, device="cuda")
+    d_par = torch.zeros(g.n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    assert _noalloc(L, d_adj.data_ptr(), g.n, d_td.data_ptr(), d_par.data_ptr(), 0, stream.cuda_stream) == 0
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0 = torch.cuda.memory_allocated()
+    for _ in range(3):
+        assert _noalloc(L, d_adj.data_ptr(), g.n, d_td.data_ptr(), d_par.data_ptr(), 0, stream.cuda_stream) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == alloc0
+    h = Handle(0)
+    td_ref, par_ref, _, _ = h.dp_solve(g.adj64(), g.n, want_order=False)
+    h.close()
+    assert int(d_td.item()) == td_ref and d_par.cpu().numpy().tolist() == par_ref.tolist()
+    bad = g.adj64().copy()
+    u = int(np.flatnonzero([(int(bad[0]) >> v) & 1 for v in range(g.n)])[0])
+    bad[u] &= ~np.uint64(1)  # edge 0-u kept only in 0's mask
+    d_bad = torch.from_numpy(bad.view(np.int64)).cuda()
+    st = _noalloc(L, d_bad.data_ptr(), g.n, d_td.data_ptr(), d_par.data_ptr(), 0, stream.cuda_stream)
+    assert st == 1  # GTD_INVALID_ARG from the device-side check
+    assert _noalloc(L, d_adj.data_ptr(), g.n, d_td.data_ptr(), d_par.data_ptr(), 0, stream.cuda_stream) == 0
+    assert int(d_td.item()) == td_ref
