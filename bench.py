@@ -344,9 +344,20 @@ def measure_dp_c3(h, steps, warmup, count=4096):
         td, pars, st = h.dp_solve_batch(graphs, packed=packed)
         host.append(time.perf_counter() - t0)
         dev.append(st["dp_ms"])
+    # the same batch with one tile size for every graph (the autotuner's best
+    # single size): what the per-n plan gains over it
+    one_size = {}
+    for lb in sorted(set(st["tile_bits_by_n"].values())) if len(set(st["tile_bits_by_n"].values())) > 1 else []:
+        h.dp_solve_batch(graphs, packed=packed, tile_bits=lb)
+        one_size[str(lb)] = statistics.median(h.dp_solve_batch(graphs, packed=packed, tile_bits=lb)[2]["dp_ms"]
+                                              for _ in range(max(3, steps // 2)))
     peak, peak_kind = peaks()
     ms = statistics.median(dev)
     return {"graphs": len(graphs), "solves_per_s": len(graphs) / (ms / 1e3), "dp_ms": ms,
+            "tile_bits_by_n": st["tile_bits_by_n"], "mixed_sizes": len(set(st["tile_bits_by_n"].values())) > 1,
+            "one_size_dp_ms": one_size,
+            "autotune_rates_subsets_per_us": {str(10 + i): [round(float(x), 1) for x in row]
+                                              for i, row in enumerate(rates)},
             "e2e_solves_per_s": len(graphs) / statistics.median(host), "alg_bytes": st["alg_bytes"],
             "alg_GBps": st["alg_bytes"] / (ms / 1e3) / 1e9, "frac_of_" + peak_kind + "_hbm":
             st["alg_bytes"] / (ms / 1e3) / 1e9 / peak, "tile_bits": st["tile_bits"], "ctas": st["ctas"],

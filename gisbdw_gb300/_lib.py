@@ -81,10 +81,13 @@ class BatchStats(ctypes.Structure):
     _fields_ = [("dp_ms", ctypes.c_float), ("total_ms", ctypes.c_float),
                 ("subsets", ctypes.c_uint64), ("alg_bytes", ctypes.c_uint64),
                 ("table_bytes", ctypes.c_uint64), ("tile_bits", ctypes.c_int),
-                ("tiles", ctypes.c_int), ("ctas", ctypes.c_int), ("graph_replayed", ctypes.c_int)]
+                ("tiles", ctypes.c_int), ("ctas", ctypes.c_int), ("graph_replayed", ctypes.c_int),
+                ("tile_bits_by_n", ctypes.c_int * (DP_MAX_N + 1))]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["tile_bits_by_n"] = {n: b for n, b in enumerate(self.tile_bits_by_n) if b}
+        return d
 
 
 _LIB = None
@@ -127,6 +130,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                                 ctypes.POINTER(BatchOpts)]
         L.gtd_dp_batch_sync.argtypes = [_vp, ctypes.POINTER(BatchStats)]
         L.gtd_dp_autotune.argtypes = [_vp, _i, _i, _vp]
+        L.gtd_dp_set_rates.argtypes = [_vp, _i, _i, _vp]
         L.gtd_abort.argtypes = [_vp]
         L.gtd_inject_fault.argtypes = [_i, _i]
         _LIB = L
@@ -253,6 +257,11 @@ class Handle:
         rates = np.zeros((n_max - n_min + 1, 5), dtype=np.float32)
         self._check(self.L.gtd_dp_autotune(self._h, n_min, n_max, _ptr(rates)))
         return rates
+
+    def dp_set_rates(self, n_min: int, rates: np.ndarray) -> None:
+        """gtd_dp_set_rates: rates rows n_min.., columns tile bits 8..12."""
+        r = np.ascontiguousarray(rates, dtype=np.float32)
+        self._check(self.L.gtd_dp_set_rates(self._h, n_min, n_min + r.shape[0] - 1, _ptr(r)))
 
     def dp_table_info(self) -> Tuple[int, int, int, int]:
         ptr, nbytes, n, lb = _vp(), _u64(), _i(), _i()

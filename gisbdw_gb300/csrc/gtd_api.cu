@@ -149,6 +149,7 @@ gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_o
   p.single.adj_off = 0;
   p.single.n = n;
   p.single.nh = L.nh;
+  p.single.lb = L.lb;
   p.single.out_idx = 0;
   p.num_graphs = 1;
   p.lb = L.lb;

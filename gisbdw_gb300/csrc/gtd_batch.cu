@@ -9,8 +9,9 @@
 // replayed while the batch keeps its shape and buffers.
 //
 // The autotuner times the DP kernel per (n, tile bits) on seeded random
-// graphs and the planner then picks, for a whole batch, the tile size with
-// the smallest predicted time (sum over graphs of padded subsets / rate).
+// graphs; the planner then gives each vertex count its own tile size
+// (pick_tile_bits) and, when the sizes differ, launches the mixed-size
+// kernel, whose tiles dispatch on their graph's size.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,7 +27,9 @@ namespace gtd {
 namespace {
 
 struct Plan {
-  int lb = 10;
+  int lb = 10;                  // the launch's (largest) tile bits
+  bool mixed = false;           // graphs carry their own tile bits
+  int lb_by_n[GTD_DP_MAX_N + 1] = {};
   std::vector<DpGraph> graphs;  // processing order
   uint64_t table_bytes = 0;
   uint32_t total_tiles = 0;
@@ -37,32 +40,81 @@ struct Plan {
 
 constexpr int kLevelSlots = kDpMaxHigh + 2;
 
-int pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const gtd_dp_batch_opts* opts) {
-  if (opts && opts->tile_bits > 0)
-    return std::min(std::max(opts->tile_bits, kTuneLbMin), kTuneLbMax);
-  int best = 10;
+// Tile bits per vertex count. An explicit opts->tile_bits gives every graph
+// that size. Otherwise, when the autotuner has rates (subsets per us of the
+// one-size kernel, measured at that kernel's own occupancy) for every n of
+// the batch, each candidate cap c = 8..12 gets, per n, the tile size
+// lb <= c with the least predicted time 2^max(n, lb) / rate(n, lb), slowed
+// by occupancy(lb) / occupancy(mixed kernel at c) where the mixed kernel
+// holds fewer CTAs; the cap with the least total time wins. One size for
+// the whole batch runs the one-size kernel. No rates: 10 bits.
+void pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const gtd_dp_batch_opts* opts, Plan& P) {
+  std::vector<int> count_by_n(GTD_DP_MAX_N + 1, 0);
+  for (int i = 0; i < count; ++i)
+    ++count_by_n[descs[i].n];
+  auto uniform = [&](int lb) {
+    P.lb = lb;
+    P.mixed = false;
+    for (int n = 0; n <= GTD_DP_MAX_N; ++n)
+      P.lb_by_n[n] = count_by_n[n] ? lb : 0;
+  };
+  if (opts && opts->tile_bits > 0) {
+    uniform(std::min(std::max(opts->tile_bits, kTuneLbMin), kTuneLbMax));
+    return;
+  }
+  for (int n = 0; n <= GTD_DP_MAX_N; ++n)
+    for (int lb = kTuneLbMin; lb <= kTuneLbMax && count_by_n[n]; ++lb)
+      if (h->tune[n][lb] <= 0) {
+        uniform(10);
+        return;
+      }
+  int occ_one[kTuneLbMax + 1] = {};
+  for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb)
+    occ_one[lb] = std::max(1, dp_tile_occupancy(lb));
   double best_cost = -1;
-  for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb) {
+  for (int c = kTuneLbMin; c <= kTuneLbMax; ++c) {
+    const int occ_mixed = dp_mixed_occupancy(c);
+    if (occ_mixed < 1)
+      continue;
+    int choice[GTD_DP_MAX_N + 1] = {};
     double cost = 0;
-    bool known = true;
-    for (int i = 0; i < count && known; ++i) {
-      const float rate = h->tune[descs[i].n][lb];
-      if (rate <= 0)
-        known = false;
-      else
-        cost += double(uint64_t(1) << std::max(descs[i].n, lb)) / rate;
+    int lo = kTuneLbMax, hi = kTuneLbMin;
+    for (int n = 0; n <= GTD_DP_MAX_N; ++n) {
+      if (!count_by_n[n])
+        continue;
+      double best_t = -1;
+      for (int lb = kTuneLbMin; lb <= c; ++lb) {
+        double t = double(uint64_t(1) << std::max(n, lb)) / h->tune[n][lb];
+        if (occ_one[lb] > occ_mixed)
+          t *= double(occ_one[lb]) / occ_mixed;
+        if (best_t < 0 || t < best_t) {
+          best_t = t;
+          choice[n] = lb;
+        }
+      }
+      cost += best_t * count_by_n[n];
+      lo = std::min(lo, choice[n]);
+      hi = std::max(hi, choice[n]);
     }
-    if (known && (best_cost < 0 || cost < best_cost)) {
+    if (lo == hi) {  // one size: the one-size kernel at its own occupancy
+      cost = 0;
+      for (int n = 0; n <= GTD_DP_MAX_N; ++n)
+        if (count_by_n[n])
+          cost += double(uint64_t(1) << std::max(n, hi)) / h->tune[n][hi] * count_by_n[n];
+    }
+    if (best_cost < 0 || cost < best_cost) {
       best_cost = cost;
-      best = lb;
+      P.lb = hi;
+      P.mixed = lo != hi;
+      for (int n = 0; n <= GTD_DP_MAX_N; ++n)
+        P.lb_by_n[n] = choice[n];
     }
   }
-  return best;
+  if (best_cost < 0)
+    uniform(10);
 }
 
-Plan make_plan(int lb, const gtd_graph_desc* descs, int count) {
-  Plan P;
-  P.lb = lb;
+void make_plan(Plan& P, const gtd_graph_desc* descs, int count) {
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return descs[a].n > descs[b].n; });
@@ -72,7 +124,9 @@ Plan make_plan(int lb, const gtd_graph_desc* descs, int count) {
   for (int k = 0; k < count; ++k) {
     const gtd_graph_desc& d = descs[order[k]];
     DpGraph& G = P.graphs[k];
+    const int lb = P.lb_by_n[d.n];
     G.n = d.n;
+    G.lb = lb;
     G.nh = d.n > lb ? d.n - lb : 0;
     G.ntiles = 1u << G.nh;
     G.table_off = off;
@@ -104,7 +158,6 @@ Plan make_plan(int lb, const gtd_graph_desc* descs, int count) {
         ticket += binom[G.nh][j];
       }
     }
-  return P;
 }
 
 uint64_t fingerprint(const Plan& P, const void* adj, const void* td, const void* par, int ctas,
@@ -114,9 +167,11 @@ uint64_t fingerprint(const Plan& P, const void* adj, const void* td, const void*
     x ^= v + 0x9e3779b97f4a7c15ull + (x << 6) + (x >> 2);
   };
   mix(P.lb);
+  mix(P.mixed);
   mix(P.graphs.size());
   for (const DpGraph& G : P.graphs) {
     mix(G.n);
+    mix(G.lb);
     mix(G.adj_off);
     mix(G.out_idx);
   }
@@ -145,10 +200,12 @@ gtd_status check_descs(gtd_handle h, const gtd_graph_desc* descs, int count, int
 // enqueues the launch (graph replay or direct). Device pointers in/out.
 gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, const uint64_t* d_adj,
                          int32_t* d_td, int32_t* d_parent, const gtd_dp_batch_opts* opts) {
-  const int lb = pick_tile_bits(h, descs, count, opts);
-  Plan P = make_plan(lb, descs, count);
+  Plan P;
+  pick_tile_bits(h, descs, count, opts, P);
+  make_plan(P, descs, count);
+  const int lb = P.lb;
   const uint64_t timeout = (opts && opts->timeout_ns) ? opts->timeout_ns : 10ull * 1000 * 1000 * 1000;
-  int occ = dp_tile_occupancy(lb);
+  int occ = P.mixed ? dp_mixed_occupancy(lb) : dp_tile_occupancy(lb);
   if (opts && opts->ctas_per_sm > 0 && opts->ctas_per_sm < occ)
     occ = opts->ctas_per_sm;
   if (occ < 1)
@@ -167,6 +224,8 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   st.tile_bits = lb;
   st.tiles = static_cast<int>(P.total_tiles);
   st.ctas = static_cast<int>(ctas);
+  for (int n = 0; n <= GTD_DP_MAX_N; ++n)
+    st.tile_bits_by_n[n] = P.lb_by_n[n];
 
   // The captured graph holds the handle's buffer addresses: replay only while
   // no other call has reallocated them (a larger single solve grows the table).
@@ -216,6 +275,7 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   bp.level_base = h->d_level_base;
   bp.num_graphs = count;
   bp.lb = lb;
+  bp.mixed = P.mixed ? 1 : 0;
   bp.total_tiles = P.total_tiles;
   bp.table = h->d_table;
   bp.flags = h->d_flags;
@@ -389,6 +449,20 @@ gtd_status gtd_dp_solve_batch(gtd_handle h, const gtd_graph_desc* descs, int cou
       std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats)
     *stats = h->bstats;
+  return GTD_OK;
+}
+
+gtd_status gtd_dp_set_rates(gtd_handle h, int n_min, int n_max, const float* rates) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!rates || n_min < 2 || n_max > GTD_DP_MAX_N || n_min > n_max)
+    return fail(h, GTD_INVALID_ARG, "rates must cover a range inside [2, " + std::to_string(GTD_DP_MAX_N) + "]");
+  for (int n = n_min; n <= n_max; ++n)
+    for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb) {
+      const float r = rates[(n - n_min) * (kTuneLbMax - kTuneLbMin + 1) + (lb - kTuneLbMin)];
+      h->tune[n][lb] = r > 0 ? r : 0.f;
+    }
+  h->bgraph_valid = false;  // a plan may change
   return GTD_OK;
 }
 

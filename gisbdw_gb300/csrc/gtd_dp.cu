@@ -219,56 +219,36 @@ __global__ void dp_fill_tile_map_kernel(const __grid_constant__ DpBatchParams p)
   }
 }
 
-template <int LB>
-__global__ void __launch_bounds__(32 * kDpWarps)
-    dp_tile_kernel(const __grid_constant__ DpBatchParams p) {
-  using Shape = TileShape<LB>;
-  constexpr int kWords = Shape::kWords;
-  constexpr int kWordBits = Shape::kWordBits;
-
-  extern __shared__ __align__(16) uint8_t smem[];
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  uint32_t* T = reinterpret_cast<uint32_t*>(smem + size_t(warp) * Shape::kPerWarp);
-  uint32_t* U = T + kWords;
-  uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + Shape::kOrderOff);
-  Binom& sBinom = *reinterpret_cast<Binom*>(smem + Shape::kBinomOff);
-  uint32_t* kids = reinterpret_cast<uint32_t*>(smem + Shape::kKidsOff) + warp * 32;
-  const Binom& binom = p.binom;
-
-  for (int i = threadIdx.x; i < (kDpMaxHigh + 1) * (kDpMaxHigh + 1); i += blockDim.x)
-    (&sBinom[0][0])[i] = (&binom[0][0])[i];
-  // Word indices ordered by popcount, colex rank inside each popcount class.
-  for (int w = threadIdx.x; w < kWords; w += blockDim.x) {
+// Word indices of `bits` bits ordered by popcount, colex rank inside each
+// popcount class. For a tile of fewer word bits the words of class s are the
+// first C(wb, s) entries of the class (colex order lists the subsets of the
+// lower positions first), so one table serves every smaller tile size.
+__device__ void build_word_order(uint16_t* sOrder, const Binom& binom, int bits) {
+  for (int w = threadIdx.x; w < (1 << bits); w += blockDim.x) {
     const int i = __popc(w);
     uint32_t pos = 0;
     for (int q = 0; q < i; ++q)
-      pos += binom[kWordBits][q];
+      pos += binom[bits][q];
     pos += rank_colex(binom, static_cast<uint32_t>(w));
     sOrder[pos] = static_cast<uint16_t>(w);
   }
-  __syncthreads();
+}
 
-  for (;;) {
-    uint32_t t = 0, gi = 0, tl = 0;
-    if (lane == 0) {
-      t = ld_relaxed_s32(p.error) != 0 ? 0xffffffffu : atomicAdd(p.ticket, 1u);
-      tl = t;
-      if (t < p.total_tiles && p.graphs) {
-        const uint2 m = __ldg(p.tile_map + t);
-        gi = m.x;
-        tl = m.y;
-      }
-    }
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= p.total_tiles)
-      break;
-    gi = __shfl_sync(0xffffffffu, gi, 0);
-    tl = __shfl_sync(0xffffffffu, tl, 0);
-    const DpGraph G = p.graphs ? p.graphs[gi] : p.single;
-    uint8_t* const table = p.table + G.table_off;
-    uint32_t* const flags = p.flags + G.tile_base;
-    const uint64_t* const adj = p.adj + G.adj_off;
+// One warp resolves local tile tl of graph G (tiles of LB bits): waits for
+// its child tiles, reduces them, resolves the tile in T / U (shared memory,
+// 2^LB / 4 words each), stores it and publishes its flag. sOrder is a word
+// order table of order_bits >= LB - 2 bits. False if a wait gave up.
+template <int LB>
+__device__ __forceinline__ bool tile_work(const DpBatchParams& p, const DpGraph& G, uint32_t tl, uint32_t* T,
+                                          uint32_t* U, const uint16_t* sOrder, int order_bits, const Binom& sBinom,
+                                          uint32_t* kids) {
+  constexpr int kWords = TileShape<LB>::kWords;
+  constexpr int kWordBits = TileShape<LB>::kWordBits;
+  const int lane = threadIdx.x & 31;
+  const Binom& binom = p.binom;
+  uint8_t* const table = p.table + G.table_off;
+  uint32_t* const flags = p.flags + G.tile_base;
+  const uint64_t* const adj = p.adj + G.adj_off;
 
     int j;
     uint32_t H, off_prev;
@@ -298,7 +278,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       ok = wait_flag(flags + child, p.epoch, p.timeout_ns, p.error);
     }
     if (__any_sync(0xffffffffu, !ok))
-      break;
+      return false;
     __syncwarp();  // kids[] written above, read by every lane below
 
     // Cross-tile children: j whole tiles, 4 subsets per word, children two
@@ -353,7 +333,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
     uint32_t start = 0;
 #pragma unroll 1
     for (int s = 0; s <= kWordBits; ++s) {
-      const uint32_t count = binom[kWordBits][s];
+      const uint32_t count = binom[kWordBits][s];  // words of this popcount class in a tile of LB bits
       for (uint32_t e = lane; e < count; e += 32) {
         const uint32_t w = sOrder[start + e];
         Acc g;
@@ -405,7 +385,7 @@ __global__ void __launch_bounds__(32 * kDpWarps)
           T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
         }
       }
-      start += count;
+      start += binom[order_bits][s];  // the order table's class sizes (order_bits >= kWordBits)
       __syncwarp();
     }
 
@@ -422,7 +402,109 @@ __global__ void __launch_bounds__(32 * kDpWarps)
     __syncwarp();
     if (lane == 0)
       st_release_u32(flags + tl, p.epoch);
+    return true;
+}
+
+// Takes the next ticket (lane 0) and maps it to (graph, local tile);
+// false when the tickets are used up or an error was raised.
+__device__ __forceinline__ bool next_tile(const DpBatchParams& p, uint32_t& gi, uint32_t& tl) {
+  const int lane = threadIdx.x & 31;
+  uint32_t t = 0;
+  gi = 0;
+  tl = 0;
+  if (lane == 0) {
+    t = ld_relaxed_s32(p.error) != 0 ? 0xffffffffu : atomicAdd(p.ticket, 1u);
+    tl = t;
+    if (t < p.total_tiles && p.graphs) {
+      const uint2 m = __ldg(p.tile_map + t);
+      gi = m.x;
+      tl = m.y;
+    }
   }
+  t = __shfl_sync(0xffffffffu, t, 0);
+  gi = __shfl_sync(0xffffffffu, gi, 0);
+  tl = __shfl_sync(0xffffffffu, tl, 0);
+  return t < p.total_tiles;
+}
+
+// Every tile of the launch has LB bits (single-graph solves, and batches
+// that use one tile size).
+template <int LB>
+__global__ void __launch_bounds__(32 * kDpWarps)
+    dp_tile_kernel(const __grid_constant__ DpBatchParams p) {
+  using Shape = TileShape<LB>;
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int warp = threadIdx.x >> 5;
+  uint32_t* T = reinterpret_cast<uint32_t*>(smem + size_t(warp) * Shape::kPerWarp);
+  uint32_t* U = T + Shape::kWords;
+  uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + Shape::kOrderOff);
+  Binom& sBinom = *reinterpret_cast<Binom*>(smem + Shape::kBinomOff);
+  uint32_t* kids = reinterpret_cast<uint32_t*>(smem + Shape::kKidsOff) + warp * 32;
+
+  for (int i = threadIdx.x; i < (kDpMaxHigh + 1) * (kDpMaxHigh + 1); i += blockDim.x)
+    (&sBinom[0][0])[i] = (&p.binom[0][0])[i];
+  build_word_order(sOrder, p.binom, Shape::kWordBits);
+  __syncthreads();
+
+  uint32_t gi, tl;
+  while (next_tile(p, gi, tl)) {
+    const DpGraph G = p.graphs ? p.graphs[gi] : p.single;
+    if (!tile_work<LB>(p, G, tl, T, U, sOrder, Shape::kWordBits, sBinom, kids))
+      break;
+  }
+}
+
+// Batches whose graphs use different tile sizes (DpGraph::lb, 8 .. p.lb):
+// shared memory is laid out for the largest (p.lb, a runtime value, so the
+// launch's occupancy follows it) and each tile dispatches on its graph's lb.
+__global__ void __launch_bounds__(32 * kDpWarps)
+    dp_tile_kernel_mixed(const __grid_constant__ DpBatchParams p) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int warp = threadIdx.x >> 5;
+  const int words = (1 << p.lb) / 4, bits = p.lb - 2;
+  const size_t per_warp = size_t(2) * words * 4;
+  const size_t order_off = kDpWarps * per_warp;
+  const size_t binom_off = (order_off + size_t(words) * 2 + 15) & ~size_t(15);
+  const size_t kids_off = (binom_off + sizeof(Binom) + 15) & ~size_t(15);
+  uint32_t* T = reinterpret_cast<uint32_t*>(smem + size_t(warp) * per_warp);
+  uint32_t* U = T + words;
+  uint16_t* sOrder = reinterpret_cast<uint16_t*>(smem + order_off);
+  Binom& sBinom = *reinterpret_cast<Binom*>(smem + binom_off);
+  uint32_t* kids = reinterpret_cast<uint32_t*>(smem + kids_off) + warp * 32;
+
+  for (int i = threadIdx.x; i < (kDpMaxHigh + 1) * (kDpMaxHigh + 1); i += blockDim.x)
+    (&sBinom[0][0])[i] = (&p.binom[0][0])[i];
+  build_word_order(sOrder, p.binom, bits);
+  __syncthreads();
+
+  uint32_t gi, tl;
+  while (next_tile(p, gi, tl)) {
+    const DpGraph G = p.graphs[gi];
+    bool ok = false;
+    if (G.lb > p.lb) {  // the planner never does this: the tile would not fit
+      raise_error(p.error, kDevInvalidInput, static_cast<int32_t>(gi));
+      break;
+    }
+    switch (G.lb) {
+      case 8: ok = tile_work<8>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
+      case 9: ok = tile_work<9>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
+      case 10: ok = tile_work<10>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
+      case 11: ok = tile_work<11>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
+      case 12: ok = tile_work<12>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
+      default: raise_error(p.error, kDevInvalidInput, static_cast<int32_t>(gi)); break;
+    }
+    if (!ok)
+      break;
+  }
+}
+
+// Dynamic shared memory of the mixed kernel for tiles of up to lb bits.
+size_t dp_mixed_smem(int lb) {
+  const size_t words = (size_t(1) << lb) / 4;
+  const size_t order_off = kDpWarps * 2 * words * 4;
+  const size_t binom_off = (order_off + words * 2 + 15) & ~size_t(15);
+  const size_t kids_off = (binom_off + sizeof(Binom) + 15) & ~size_t(15);
+  return kids_off + size_t(kDpWarps) * 32 * 4;
 }
 
 // ---------------------------------------------------------------------------
@@ -507,7 +589,7 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
     for (int v = lane; v < n; v += 32)
       sAdj[v] = p.adj[G.adj_off + v];
     __syncwarp();
-    const TreeCtx ctx{p.binom, p.table + G.table_off, p.lb, G.nh, n};
+    const TreeCtx ctx{p.binom, p.table + G.table_off, G.lb, G.nh, n};
     const uint64_t query = p.query ? p.query : (n == 64 ? ~0ull : ((1ull << n) - 1));
     const uint32_t td = query ? ctx.td_of(query) : 0u;
     if (lane == 0 && p.td_out)
@@ -650,7 +732,23 @@ cudaError_t dp_launch_fill_tile_map(const DpBatchParams& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+int dp_mixed_occupancy(int lb) {
+  const size_t smem = dp_mixed_smem(lb);
+  if (cudaFuncSetAttribute(dp_tile_kernel_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(dp_mixed_smem(kDpMaxTileBits))) != cudaSuccess)
+    return 0;
+  int blocks = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, dp_tile_kernel_mixed, 32 * kDpWarps, smem);
+  return blocks;
+}
+
 cudaError_t dp_launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s) {
+  if (p.mixed) {
+    if (p.lb < kDpMinTileBits || p.lb > kDpMaxTileBits)
+      return cudaErrorInvalidValue;
+    dp_tile_kernel_mixed<<<ctas, 32 * kDpWarps, dp_mixed_smem(p.lb), s>>>(p);
+    return cudaGetLastError();
+  }
   switch (p.lb) {
 #define GTD_CASE(X) \
   case X:           \
@@ -679,7 +777,7 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
                      uint64_t* roots_out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const DpGraph G = p.single;
-  const TreeCtx ctx{p.binom, p.table + G.table_off, p.lb, G.nh, G.n};
+  const TreeCtx ctx{p.binom, p.table + G.table_off, G.lb, G.nh, G.n};
   for (int i = blockIdx.x * kTreeWarps + warp; i < count; i += gridDim.x * kTreeWarps) {
     const uint64_t S = subsets[i];
     if (S == 0) {

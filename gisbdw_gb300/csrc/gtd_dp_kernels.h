@@ -9,7 +9,7 @@
 
 namespace gtd {
 
-// One graph of a DP launch (32 bytes). A graph with n < lb is padded with
+// One graph of a DP launch (40 bytes). A graph with n < lb is padded with
 // isolated vertices up to lb (one tile); padding changes no treedepth of a
 // real subset and the reconstruction never touches padded vertices.
 struct DpGraph {
@@ -20,6 +20,7 @@ struct DpGraph {
   int32_t n = 0;           // real vertices
   int32_t nh = 0;          // high vertices (max(n - lb, 0))
   int32_t out_idx = 0;     // position of the graph in the caller's arrays (td_out)
+  int32_t lb = 0;          // tile bits of this graph's table
 };
 
 // Passed by value as a __grid_constant__ kernel parameter: the binomial
@@ -31,7 +32,8 @@ struct DpBatchParams {
   uint2* tile_map = nullptr;        // ticket -> (graph, local tile) (batches)
   const uint32_t* level_base = nullptr;  // [graph][level] first ticket (batches)
   int num_graphs = 1;
-  int lb = 0;                       // tile bits of this launch
+  int lb = 0;                       // tile bits of this launch (mixed batches: the largest)
+  int mixed = 0;                    // 1: graphs carry their own tile bits (DpGraph::lb)
   uint32_t total_tiles = 0;
   uint8_t* table = nullptr;         // table pool
   uint32_t* flags = nullptr;        // one ready stamp per global tile
@@ -50,6 +52,8 @@ struct DpBatchParams {
 
 void dp_fill_binom(DpBatchParams& p);
 int dp_tile_occupancy(int lb);
+// CTAs per SM of the mixed-tile-size kernel with tiles of up to lb bits.
+int dp_mixed_occupancy(int lb);
 cudaError_t dp_launch_validate(const DpBatchParams& p, cudaStream_t s);
 cudaError_t dp_launch_fill_tile_map(const DpBatchParams& p, cudaStream_t s);
 cudaError_t dp_launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s);

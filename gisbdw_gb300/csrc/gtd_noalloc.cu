@@ -99,6 +99,7 @@ extern "C" gtd_status gtd_dp_solve_noalloc(const uint64_t* d_adj, int n, int32_t
   p.single.ntiles = L.ntiles;
   p.single.n = n;
   p.single.nh = L.nh;
+  p.single.lb = L.lb;
   p.num_graphs = 1;
   p.lb = L.lb;
   p.total_tiles = L.ntiles;

@@ -144,7 +144,8 @@ typedef struct {
 } gtd_graph_desc;
 
 typedef struct {
-  int tile_bits;        /* 8..12; 0 = from gtd_dp_autotune, else 10 */
+  int tile_bits;        /* 8..12 for every graph; 0 = per vertex count from
+                           gtd_dp_autotune's rates (else 10) */
   int ctas_per_sm;      /* 0 = occupancy limit */
   uint64_t timeout_ns;  /* bound on every in-kernel wait (0 = 10 s) */
   int use_cuda_graph;   /* capture the launch once, replay while the batch
@@ -157,10 +158,12 @@ typedef struct {
   uint64_t subsets;     /* sum of 2^n over the batch */
   uint64_t alg_bytes;   /* sum of 2^n + n 2^(n-1) */
   uint64_t table_bytes; /* table pool (graphs with n < tile bits padded) */
-  int tile_bits;
+  int tile_bits;        /* the launch's largest tile size */
   int tiles;
   int ctas;
   int graph_replayed;   /* 1 if an existing CUDA graph was replayed */
+  int tile_bits_by_n[GTD_DP_MAX_N + 1]; /* tile size of the graphs with n
+                                           vertices (0: none in the batch) */
 } gtd_dp_batch_stats;
 
 /* DynamicGPU over many graphs of uneven size in ONE persistent launch
@@ -189,11 +192,20 @@ gtd_status gtd_dp_batch_sync(gtd_handle h, gtd_dp_batch_stats* stats);
 /* The autotuner: times the batched DP kernel for every n in [n_min, n_max]
  * and tile bits 8..12 on seeded random graphs (at least 2^26 subsets per
  * measurement) and keeps the rates in the handle; batches solved with
- * tile_bits = 0 then use the tile size with the least predicted time.
+ * tile_bits = 0 then give each vertex count the tile size with the least
+ * predicted time (graphs of different sizes share one launch; the launch's
+ * occupancy follows its largest tile, which the prediction accounts for).
  * rates_out (may be NULL) receives (n_max - n_min + 1) x 5 rates in subsets
  * per microsecond, row n, column tile bits - 8. */
 gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max,
                            float* rates_out);
+
+/* Loads autotuner rates (the layout gtd_dp_autotune writes: rows n_min ..
+ * n_max, columns tile bits 8..12, subsets per microsecond; 0 = unknown),
+ * e.g. saved from an earlier process, so that a handle plans batches
+ * without measuring again. 2 <= n_min <= n_max <= GTD_DP_MAX_N. */
+gtd_status gtd_dp_set_rates(gtd_handle h, int n_min, int n_max,
+                            const float* rates);
 
 /* ---- Branch and bound -------------------------------------------------- */
 

@@ -72,3 +72,40 @@ def test_autotune_then_batch(handle, port):
     assert 8 <= stats["tile_bits"] <= 12
     for g, t in zip(gs, td):
         assert t == port.dp_solve(g)[0]
+
+
+def _rates_favouring(choice, n_min=2, n_max=24):
+    """Synthetic autotuner rates (rows n_min..n_max, columns tile bits 8..12)
+    that make the planner pick choice(n) tile bits for n vertices."""
+    r = np.ones((n_max - n_min + 1, 5), dtype=np.float32)
+    for n in range(n_min, n_max + 1):
+        r[n - n_min, choice(n) - 8] = 1e4
+    return r
+
+
+@pytest.mark.parametrize("choice", [lambda n: 8 if n <= 16 else 12,
+                                    lambda n: 9 + n % 3,
+                                    lambda n: 11 if n >= 20 else 10])
+def test_batch_tile_bits_per_n_match_oracle(port, choice):
+    """Tile sizes per vertex count in one launch (the mixed-size kernel):
+    every graph bit-exact against the oracle, the plan reported per n, and a
+    CUDA-graph replay with new contents still exact."""
+    from gisbdw_gb300 import Handle
+    h = Handle(0)
+    h.dp_set_rates(2, _rates_favouring(choice))
+    gs = mixed_batch() + [G.gnp_connected(n, 0.3, 40 + n) for n in range(8, 25)]
+    gs = [g for g in gs if g.n >= 2]
+    td, parents, stats = h.dp_solve_batch(gs)
+    want = {g.n: choice(g.n) for g in gs}
+    assert stats["tile_bits_by_n"] == want
+    assert stats["tile_bits"] == max(want.values())
+    for g, t, par in zip(gs, td, parents):
+        otd, opar = port.dp_solve(g)
+        assert t == otd and par.tolist() == opar.tolist(), g.name
+    other = [G.relabel(g, list(reversed(range(g.n)))) for g in gs]
+    td2, par2, st2 = h.dp_solve_batch(other)
+    assert st2["graph_replayed"] == 1
+    for g, t, par in zip(other, td2, par2):
+        otd, opar = port.dp_solve(g)
+        assert t == otd and par.tolist() == opar.tolist(), g.name
+    h.close()

@@ -62,7 +62,8 @@ def test_allocation_failure_batch_and_bnb(fresh):
     _lib.inject_fault(_lib.FAULT_NONE, 0)
     res = fresh.bnb_solve_batch(more, deadline_ns=30 * 10**9)
     assert np.all(res["status"] == 0)
-    assert res["td"][:2].tolist() == bref["td"].tolist() and res["td"][2:].tolist() == [5, 4]
+    dtd, _, _ = fresh.dp_solve_batch(more)
+    assert res["td"][:2].tolist() == bref["td"].tolist() and res["td"].tolist() == dtd.tolist()
 
 
 def test_class_layer_swallows_oom_like_the_reference():
