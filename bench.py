@@ -317,16 +317,18 @@ def run_reference(args, graphs):
 # GPU arm.
 # ---------------------------------------------------------------------------
 
-def measure_dp_c3(h, steps, warmup, count=4096):
+def measure_dp_c3(h, steps, warmup, count=4096, device=0):
     """Batched uneven DP on config 3 (4096 graphs), device time from the
     library's events and host time of the whole C-ABI call."""
+    import numpy as np
+
     from gisbdw_gb300 import _lib
     from gisbdw_gb300 import graphs as G
     from gisbdw_gb300.validate import check_tree
     graphs = G.config3_graphs(count=count)
     packed = _lib.pack_batch(graphs)
     t0 = time.perf_counter()
-    rates = h.dp_autotune(10, 24)  # subsets/us per (n, tile bits 8..12); the planner picks from these
+    rates, mixed_eff = h.dp_autotune(10, 24, with_mixed=True)  # subsets/us per (n, tile bits 8..12)
     tune_s = time.perf_counter() - t0
     for _ in range(warmup):
         td, pars, st = h.dp_solve_batch(graphs, packed=packed)
@@ -344,20 +346,31 @@ def measure_dp_c3(h, steps, warmup, count=4096):
         td, pars, st = h.dp_solve_batch(graphs, packed=packed)
         host.append(time.perf_counter() - t0)
         dev.append(st["dp_ms"])
-    # the same batch with one tile size for every graph (the autotuner's best
-    # single size): what the per-n plan gains over it
+    # the same batch at every single tile size, and with each n at its own
+    # best size (mixed-size kernel, forced): what the plan chose against
     one_size = {}
-    for lb in sorted(set(st["tile_bits_by_n"].values())) if len(set(st["tile_bits_by_n"].values())) > 1 else []:
+    for lb in range(8, 13):
         h.dp_solve_batch(graphs, packed=packed, tile_bits=lb)
         one_size[str(lb)] = statistics.median(h.dp_solve_batch(graphs, packed=packed, tile_bits=lb)[2]["dp_ms"]
                                               for _ in range(max(3, steps // 2)))
+    per_n_best = {}
+    h2 = type(h)(device)
+    try:
+        h2.dp_set_rates(10, rates, mixed_eff=np.ones(5))  # efficiency 1: the per-n optimum, mixed
+        h2.dp_solve_batch(graphs, packed=packed)
+        runs = [h2.dp_solve_batch(graphs, packed=packed)[2] for _ in range(max(3, steps // 2))]
+        per_n_best = {"dp_ms": statistics.median(r["dp_ms"] for r in runs),
+                      "tile_bits_by_n": runs[-1]["tile_bits_by_n"]}
+    finally:
+        h2.close()
     peak, peak_kind = peaks()
     ms = statistics.median(dev)
     return {"graphs": len(graphs), "solves_per_s": len(graphs) / (ms / 1e3), "dp_ms": ms,
             "tile_bits_by_n": st["tile_bits_by_n"], "mixed_sizes": len(set(st["tile_bits_by_n"].values())) > 1,
-            "one_size_dp_ms": one_size,
+            "one_size_dp_ms": one_size, "per_n_best_mixed_kernel": per_n_best,
             "autotune_rates_subsets_per_us": {str(10 + i): [round(float(x), 1) for x in row]
                                               for i, row in enumerate(rates)},
+            "autotune_mixed_kernel_efficiency": [round(float(x), 3) for x in mixed_eff],
             "e2e_solves_per_s": len(graphs) / statistics.median(host), "alg_bytes": st["alg_bytes"],
             "alg_GBps": st["alg_bytes"] / (ms / 1e3) / 1e9, "frac_of_" + peak_kind + "_hbm":
             st["alg_bytes"] / (ms / 1e3) / 1e9 / peak, "tile_bits": st["tile_bits"], "ctas": st["ctas"],
@@ -583,7 +596,7 @@ def run_gpu(args, graphs):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_c3:
-        line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup, args.c3_graphs)
+        line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup, args.c3_graphs, local)
     if rank == 0 and not args.no_bnb:
         line["bnb_c4"] = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
                                      0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes)

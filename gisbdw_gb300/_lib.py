@@ -129,8 +129,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.gtd_dp_solve_batch_device.argtypes = [_vp, _vp, _i, _vp, ctypes.c_int64, _vp, _vp,
                                                 ctypes.POINTER(BatchOpts)]
         L.gtd_dp_batch_sync.argtypes = [_vp, ctypes.POINTER(BatchStats)]
-        L.gtd_dp_autotune.argtypes = [_vp, _i, _i, _vp]
-        L.gtd_dp_set_rates.argtypes = [_vp, _i, _i, _vp]
+        L.gtd_dp_autotune.argtypes = [_vp, _i, _i, _vp, _vp]
+        L.gtd_dp_set_rates.argtypes = [_vp, _i, _i, _vp, _vp]
         L.gtd_abort.argtypes = [_vp]
         L.gtd_inject_fault.argtypes = [_i, _i]
         _LIB = L
@@ -252,16 +252,22 @@ class Handle:
         self._check(self.L.gtd_dp_batch_sync(self._h, ctypes.byref(stats)))
         return stats.as_dict()
 
-    def dp_autotune(self, n_min: int, n_max: int) -> np.ndarray:
-        """Rates (subsets per microsecond), rows n_min..n_max, columns tile bits 8..12."""
+    def dp_autotune(self, n_min: int, n_max: int, with_mixed: bool = False):
+        """Rates (subsets per microsecond), rows n_min..n_max, columns tile
+        bits 8..12; with_mixed: also the mixed-size kernel's efficiency per
+        largest tile size 8..12 (returns (rates, eff))."""
         rates = np.zeros((n_max - n_min + 1, 5), dtype=np.float32)
-        self._check(self.L.gtd_dp_autotune(self._h, n_min, n_max, _ptr(rates)))
-        return rates
+        eff = np.zeros(5, dtype=np.float32)
+        self._check(self.L.gtd_dp_autotune(self._h, n_min, n_max, _ptr(rates), _ptr(eff)))
+        return (rates, eff) if with_mixed else rates
 
-    def dp_set_rates(self, n_min: int, rates: np.ndarray) -> None:
-        """gtd_dp_set_rates: rates rows n_min.., columns tile bits 8..12."""
+    def dp_set_rates(self, n_min: int, rates: np.ndarray, mixed_eff=None) -> None:
+        """gtd_dp_set_rates: rates rows n_min.., columns tile bits 8..12;
+        mixed_eff: 5 efficiencies of the mixed-size kernel (None: never mix)."""
         r = np.ascontiguousarray(rates, dtype=np.float32)
-        self._check(self.L.gtd_dp_set_rates(self._h, n_min, n_min + r.shape[0] - 1, _ptr(r)))
+        e = np.ascontiguousarray(mixed_eff, dtype=np.float32) if mixed_eff is not None else None
+        self._check(self.L.gtd_dp_set_rates(self._h, n_min, n_min + r.shape[0] - 1, _ptr(r),
+                                            _ptr(e) if e is not None else None))
 
     def dp_table_info(self) -> Tuple[int, int, int, int]:
         ptr, nbytes, n, lb = _vp(), _u64(), _i(), _i()

@@ -42,13 +42,15 @@ constexpr int kLevelSlots = kDpMaxHigh + 2;
 
 // Tile bits per vertex count. An explicit opts->tile_bits gives every graph
 // that size. Otherwise, when the autotuner has rates (subsets per us of the
-// one-size kernel, measured at that kernel's own occupancy) for every n of
-// the batch, each candidate cap c = 8..12 gets, per n, the tile size
-// lb <= c with the least predicted time 2^max(n, lb) / rate(n, lb), slowed
-// by occupancy(lb) / occupancy(mixed kernel at c) where the mixed kernel
-// holds fewer CTAs; the cap with the least total time wins. One size for
-// the whole batch runs the one-size kernel. No rates: 10 bits.
-void pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const gtd_dp_batch_opts* opts, Plan& P) {
+// one-size kernel) for every n of the batch, the candidates are one size lb
+// for all graphs (predicted time sum 2^max(n, lb) / rate(n, lb)) and, per cap
+// c = 8..12, each n's own best size lb <= c run by the mixed-size kernel
+// (the same sum over the chosen sizes, divided by the mixed kernel's
+// measured efficiency at cap c); the least predicted time wins. No rates:
+// 10 bits. force_cap > 0 (the autotuner's own measurement) plans a mixed
+// launch at that cap.
+void pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const gtd_dp_batch_opts* opts, Plan& P,
+                    int force_cap = 0) {
   std::vector<int> count_by_n(GTD_DP_MAX_N + 1, 0);
   for (int i = 0; i < count; ++i)
     ++count_by_n[descs[i].n];
@@ -58,6 +60,11 @@ void pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const 
     for (int n = 0; n <= GTD_DP_MAX_N; ++n)
       P.lb_by_n[n] = count_by_n[n] ? lb : 0;
   };
+  if (force_cap > 0) {
+    uniform(force_cap);
+    P.mixed = true;
+    return;
+  }
   if (opts && opts->tile_bits > 0) {
     uniform(std::min(std::max(opts->tile_bits, kTuneLbMin), kTuneLbMax));
     return;
@@ -68,50 +75,44 @@ void pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const 
         uniform(10);
         return;
       }
-  int occ_one[kTuneLbMax + 1] = {};
-  for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb)
-    occ_one[lb] = std::max(1, dp_tile_occupancy(lb));
+  auto t_of = [&](int n, int lb) { return double(uint64_t(1) << std::max(n, lb)) / h->tune[n][lb]; };
   double best_cost = -1;
+  for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb) {
+    double cost = 0;
+    for (int n = 0; n <= GTD_DP_MAX_N; ++n)
+      if (count_by_n[n])
+        cost += t_of(n, lb) * count_by_n[n];
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      uniform(lb);
+    }
+  }
   for (int c = kTuneLbMin; c <= kTuneLbMax; ++c) {
-    const int occ_mixed = dp_mixed_occupancy(c);
-    if (occ_mixed < 1)
-      continue;
+    const float eff = h->tune_mixed_eff[c];
+    if (eff <= 0)
+      continue;  // unmeasured: never mix at this cap
     int choice[GTD_DP_MAX_N + 1] = {};
     double cost = 0;
     int lo = kTuneLbMax, hi = kTuneLbMin;
     for (int n = 0; n <= GTD_DP_MAX_N; ++n) {
       if (!count_by_n[n])
         continue;
-      double best_t = -1;
-      for (int lb = kTuneLbMin; lb <= c; ++lb) {
-        double t = double(uint64_t(1) << std::max(n, lb)) / h->tune[n][lb];
-        if (occ_one[lb] > occ_mixed)
-          t *= double(occ_one[lb]) / occ_mixed;
-        if (best_t < 0 || t < best_t) {
-          best_t = t;
+      for (int lb = kTuneLbMin; lb <= c; ++lb)
+        if (!choice[n] || t_of(n, lb) < t_of(n, choice[n]))
           choice[n] = lb;
-        }
-      }
-      cost += best_t * count_by_n[n];
+      cost += t_of(n, choice[n]) * count_by_n[n];
       lo = std::min(lo, choice[n]);
       hi = std::max(hi, choice[n]);
     }
-    if (lo == hi) {  // one size: the one-size kernel at its own occupancy
-      cost = 0;
-      for (int n = 0; n <= GTD_DP_MAX_N; ++n)
-        if (count_by_n[n])
-          cost += double(uint64_t(1) << std::max(n, hi)) / h->tune[n][hi] * count_by_n[n];
-    }
-    if (best_cost < 0 || cost < best_cost) {
+    cost /= eff;
+    if (lo != hi && hi == c && cost < best_cost) {
       best_cost = cost;
-      P.lb = hi;
-      P.mixed = lo != hi;
+      P.lb = c;
+      P.mixed = true;
       for (int n = 0; n <= GTD_DP_MAX_N; ++n)
         P.lb_by_n[n] = choice[n];
     }
   }
-  if (best_cost < 0)
-    uniform(10);
 }
 
 void make_plan(Plan& P, const gtd_graph_desc* descs, int count) {
@@ -199,9 +200,9 @@ gtd_status check_descs(gtd_handle h, const gtd_graph_desc* descs, int count, int
 // Plans the batch, (re)builds device state when the shape changed and
 // enqueues the launch (graph replay or direct). Device pointers in/out.
 gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, const uint64_t* d_adj,
-                         int32_t* d_td, int32_t* d_parent, const gtd_dp_batch_opts* opts) {
+                         int32_t* d_td, int32_t* d_parent, const gtd_dp_batch_opts* opts, int force_cap = 0) {
   Plan P;
-  pick_tile_bits(h, descs, count, opts, P);
+  pick_tile_bits(h, descs, count, opts, P, force_cap);
   make_plan(P, descs, count);
   const int lb = P.lb;
   const uint64_t timeout = (opts && opts->timeout_ns) ? opts->timeout_ns : 10ull * 1000 * 1000 * 1000;
@@ -377,6 +378,14 @@ void random_graph(int n, uint64_t seed, uint64_t* adj) {
 }  // namespace
 }  // namespace gtd
 
+namespace gtd {
+namespace {
+gtd_status solve_batch_host(gtd_handle h, const gtd_graph_desc* descs, int count, const uint64_t* adj_pool,
+                            int64_t pool_len, int32_t* td_out, int32_t* parent_out, const gtd_dp_batch_opts* opts,
+                            gtd_dp_batch_stats* stats, int force_cap);
+}  // namespace
+}  // namespace gtd
+
 using namespace gtd;
 
 extern "C" {
@@ -405,6 +414,17 @@ gtd_status gtd_dp_batch_sync(gtd_handle h, gtd_dp_batch_stats* stats) {
 gtd_status gtd_dp_solve_batch(gtd_handle h, const gtd_graph_desc* descs, int count, const uint64_t* adj_pool,
                               int64_t pool_len, int32_t* td_out, int32_t* parent_out,
                               const gtd_dp_batch_opts* opts, gtd_dp_batch_stats* stats) {
+  return solve_batch_host(h, descs, count, adj_pool, pool_len, td_out, parent_out, opts, stats, 0);
+}
+
+}  // extern "C"
+
+namespace gtd {
+namespace {
+
+gtd_status solve_batch_host(gtd_handle h, const gtd_graph_desc* descs, int count, const uint64_t* adj_pool,
+                            int64_t pool_len, int32_t* td_out, int32_t* parent_out, const gtd_dp_batch_opts* opts,
+                            gtd_dp_batch_stats* stats, int force_cap) {
   if (!h)
     return GTD_INVALID_ARG;
   gtd_status s = check_descs(h, descs, count, pool_len);
@@ -431,7 +451,7 @@ gtd_status gtd_dp_solve_batch(gtd_handle h, const gtd_graph_desc* descs, int cou
   char* stage = static_cast<char*>(h->h_bstage);
   std::memcpy(stage, adj_pool, adj_bytes);
   GTD_CUDA(h, cudaMemcpyAsync(h->d_badj, stage, adj_bytes, cudaMemcpyHostToDevice, h->stream));
-  s = batch_enqueue(h, descs, count, h->d_badj, h->d_btd, h->d_bparent, opts);
+  s = batch_enqueue(h, descs, count, h->d_badj, h->d_btd, h->d_bparent, opts, force_cap);
   if (s != GTD_OK)
     return s;
   int32_t* h_td = reinterpret_cast<int32_t*>(stage + adj_bytes);
@@ -452,7 +472,12 @@ gtd_status gtd_dp_solve_batch(gtd_handle h, const gtd_graph_desc* descs, int cou
   return GTD_OK;
 }
 
-gtd_status gtd_dp_set_rates(gtd_handle h, int n_min, int n_max, const float* rates) {
+}  // namespace
+}  // namespace gtd
+
+extern "C" {
+
+gtd_status gtd_dp_set_rates(gtd_handle h, int n_min, int n_max, const float* rates, const float* mixed_eff) {
   if (!h)
     return GTD_INVALID_ARG;
   if (!rates || n_min < 2 || n_max > GTD_DP_MAX_N || n_min > n_max)
@@ -462,11 +487,13 @@ gtd_status gtd_dp_set_rates(gtd_handle h, int n_min, int n_max, const float* rat
       const float r = rates[(n - n_min) * (kTuneLbMax - kTuneLbMin + 1) + (lb - kTuneLbMin)];
       h->tune[n][lb] = r > 0 ? r : 0.f;
     }
+  for (int c = kTuneLbMin; c <= kTuneLbMax; ++c)
+    h->tune_mixed_eff[c] = (mixed_eff && mixed_eff[c - kTuneLbMin] > 0) ? mixed_eff[c - kTuneLbMin] : 0.f;
   h->bgraph_valid = false;  // a plan may change
   return GTD_OK;
 }
 
-gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max, float* rates_out) {
+gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max, float* rates_out, float* mixed_eff_out) {
   if (!h)
     return GTD_INVALID_ARG;
   if (n_min < 2 || n_max > 30 || n_min > n_max)
@@ -483,22 +510,32 @@ gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max, float* rates_out)
     }
     const int64_t pool = int64_t(count) * n;
     std::vector<int32_t> td(count), par(pool);
-    for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb) {
-      gtd_dp_batch_opts o{lb, 0, 0, 1};
-      gtd_dp_batch_stats st{};
-      float best = 0;
-      for (int rep = 0; rep < 3; ++rep) {
-        gtd_status s = gtd_dp_solve_batch(h, descs.data(), count, adj.data(), pool, td.data(), par.data(), &o, &st);
-        if (s != GTD_OK)
-          return s;
-        if (rep > 0 && (best == 0 || st.dp_ms < best))
-          best = st.dp_ms;
+    // the one-size kernel at every tile size; at n_max also the mixed-size
+    // kernel at every cap (all graphs at that size), for its efficiency
+    for (int pass = 0; pass < (n == n_max ? 2 : 1); ++pass)
+      for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb) {
+        gtd_dp_batch_opts o{lb, 0, 0, 1};
+        gtd_dp_batch_stats st{};
+        float best = 0;
+        for (int rep = 0; rep < 3; ++rep) {
+          gtd_status s = solve_batch_host(h, descs.data(), count, adj.data(), pool, td.data(), par.data(),
+                                          pass ? nullptr : &o, &st, pass ? lb : 0);
+          if (s != GTD_OK)
+            return s;
+          if (rep > 0 && (best == 0 || st.dp_ms < best))
+            best = st.dp_ms;
+        }
+        const float rate = best > 0 ? float(double(st.subsets) / (best * 1000.0)) : 0.f;  // per microsecond
+        if (pass == 0) {
+          h->tune[n][lb] = rate;
+          if (rates_out)
+            rates_out[(n - n_min) * (kTuneLbMax - kTuneLbMin + 1) + (lb - kTuneLbMin)] = rate;
+        } else {
+          h->tune_mixed_eff[lb] = h->tune[n][lb] > 0 ? rate / h->tune[n][lb] : 0.f;
+          if (mixed_eff_out)
+            mixed_eff_out[lb - kTuneLbMin] = h->tune_mixed_eff[lb];
+        }
       }
-      const float rate = best > 0 ? float(double(st.subsets) / (best * 1000.0)) : 0.f;  // per microsecond
-      h->tune[n][lb] = rate;
-      if (rates_out)
-        rates_out[(n - n_min) * (kTuneLbMax - kTuneLbMin + 1) + (lb - kTuneLbMin)] = rate;
-    }
   }
   return GTD_OK;
 }

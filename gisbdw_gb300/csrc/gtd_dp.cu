@@ -457,6 +457,10 @@ __global__ void __launch_bounds__(32 * kDpWarps)
 // Batches whose graphs use different tile sizes (DpGraph::lb, 8 .. p.lb):
 // shared memory is laid out for the largest (p.lb, a runtime value, so the
 // launch's occupancy follows it) and each tile dispatches on its graph's lb.
+// The five inlined tile sizes raise the register count (62 against 48 for
+// one size), so this kernel holds fewer CTAs than the one-size kernel; the
+// autotuner measures that cost and the planner only mixes sizes when the
+// per-size gains outweigh it.
 __global__ void __launch_bounds__(32 * kDpWarps)
     dp_tile_kernel_mixed(const __grid_constant__ DpBatchParams p) {
   extern __shared__ __align__(16) uint8_t smem[];

@@ -77,6 +77,9 @@ struct gtd_handle_s {
   gtd_dp_batch_stats bstats = {};
   // Autotuner: subsets per millisecond by n and tile bits (0 = unmeasured).
   float tune[GTD_DP_MAX_N + 1][gtd::kTuneLbMax + 1] = {};
+  // Mixed-size kernel throughput over the one-size kernel's, per largest tile
+  // size (0 = unmeasured), from the autotuner.
+  float tune_mixed_eff[gtd::kTuneLbMax + 1] = {};
 
   gtd_bnb_state* bnb = nullptr;
   void* d_scratch = nullptr;  // general device scratch (labels, GNN batches)

@@ -144,8 +144,8 @@ typedef struct {
 } gtd_graph_desc;
 
 typedef struct {
-  int tile_bits;        /* 8..12 for every graph; 0 = per vertex count from
-                           gtd_dp_autotune's rates (else 10) */
+  int tile_bits;        /* 8..12 for every graph; 0 = planned per vertex
+                           count from gtd_dp_autotune's results (else 10) */
   int ctas_per_sm;      /* 0 = occupancy limit */
   uint64_t timeout_ns;  /* bound on every in-kernel wait (0 = 10 s) */
   int use_cuda_graph;   /* capture the launch once, replay while the batch
@@ -191,21 +191,23 @@ gtd_status gtd_dp_batch_sync(gtd_handle h, gtd_dp_batch_stats* stats);
 
 /* The autotuner: times the batched DP kernel for every n in [n_min, n_max]
  * and tile bits 8..12 on seeded random graphs (at least 2^26 subsets per
- * measurement) and keeps the rates in the handle; batches solved with
- * tile_bits = 0 then give each vertex count the tile size with the least
- * predicted time (graphs of different sizes share one launch; the launch's
- * occupancy follows its largest tile, which the prediction accounts for).
- * rates_out (may be NULL) receives (n_max - n_min + 1) x 5 rates in subsets
- * per microsecond, row n, column tile bits - 8. */
+ * measurement) and keeps the rates in the handle; rates_out (may be NULL)
+ * receives (n_max - n_min + 1) x 5 rates in subsets per microsecond, row n,
+ * column tile bits - 8. At n_max it also times the mixed-size kernel (the
+ * one that runs graphs of different tile sizes in one launch; it holds fewer
+ * CTAs per SM) at each largest tile size 8..12: mixed_eff_out (may be NULL)
+ * receives its 5 throughputs relative to the one-size kernel. Batches solved
+ * with tile_bits = 0 then give each vertex count its own tile size when the
+ * predicted time, mixed-kernel efficiency included, beats one size for all. */
 gtd_status gtd_dp_autotune(gtd_handle h, int n_min, int n_max,
-                           float* rates_out);
+                           float* rates_out, float* mixed_eff_out);
 
-/* Loads autotuner rates (the layout gtd_dp_autotune writes: rows n_min ..
- * n_max, columns tile bits 8..12, subsets per microsecond; 0 = unknown),
- * e.g. saved from an earlier process, so that a handle plans batches
- * without measuring again. 2 <= n_min <= n_max <= GTD_DP_MAX_N. */
+/* Loads autotuner results (the layouts gtd_dp_autotune writes; 0 =
+ * unknown; mixed_eff may be NULL: never mix sizes), e.g. saved from an
+ * earlier process, so that a handle plans batches without measuring again.
+ * 2 <= n_min <= n_max <= GTD_DP_MAX_N. */
 gtd_status gtd_dp_set_rates(gtd_handle h, int n_min, int n_max,
-                            const float* rates);
+                            const float* rates, const float* mixed_eff);
 
 /* ---- Branch and bound -------------------------------------------------- */
 

@@ -65,8 +65,9 @@ def test_batch_rejects_invalid_member(handle):
 
 
 def test_autotune_then_batch(handle, port):
-    rates = handle.dp_autotune(10, 12)
+    rates, eff = handle.dp_autotune(10, 12, with_mixed=True)
     assert rates.shape == (3, 5) and np.all(rates > 0)
+    assert eff.shape == (5,) and np.all(eff > 0)
     gs = [G.gnp_connected(n, 0.3, n) for n in (10, 11, 12)]
     td, parents, stats = handle.dp_solve_batch(gs)
     assert 8 <= stats["tile_bits"] <= 12
@@ -92,7 +93,7 @@ def test_batch_tile_bits_per_n_match_oracle(port, choice):
     CUDA-graph replay with new contents still exact."""
     from gisbdw_gb300 import Handle
     h = Handle(0)
-    h.dp_set_rates(2, _rates_favouring(choice))
+    h.dp_set_rates(2, _rates_favouring(choice), mixed_eff=np.ones(5))
     gs = mixed_batch() + [G.gnp_connected(n, 0.3, 40 + n) for n in range(8, 25)]
     gs = [g for g in gs if g.n >= 2]
     td, parents, stats = h.dp_solve_batch(gs)
@@ -108,4 +109,20 @@ def test_batch_tile_bits_per_n_match_oracle(port, choice):
     for g, t, par in zip(other, td2, par2):
         otd, opar = port.dp_solve(g)
         assert t == otd and par.tolist() == opar.tolist(), g.name
+    h.close()
+
+
+def test_planner_never_mixes_without_a_measured_gain(port):
+    """Rates favouring different sizes per n but a mixed-kernel efficiency
+    that eats the gain: one size for every graph."""
+    from gisbdw_gb300 import Handle
+    h = Handle(0)
+    r = _rates_favouring(lambda n: 10 if n <= 16 else 11)
+    r[r == 1] = 9e3  # every size nearly as good
+    h.dp_set_rates(2, r, mixed_eff=np.full(5, 0.5))
+    gs = [G.gnp_connected(n, 0.3, 60 + n) for n in range(12, 22)]
+    td, parents, stats = h.dp_solve_batch(gs)
+    assert len(set(stats["tile_bits_by_n"].values())) == 1
+    for g, t in zip(gs, td):
+        assert t == port.dp_solve(g)[0]
     h.close()
