@@ -377,6 +377,27 @@ def _heuristic_batch(self, graphs, kind: int = 0, scores=None):
 Handle.heuristic_batch = _heuristic_batch
 
 
+BOTTOM_UP_MAX_N = 32
+
+
+def _bottom_up(self, g):
+    """gtd_bottom_up: the reference's bottom-up union-find heuristic DP on
+    the GPU (n <= 32). Returns (td, parent, order)."""
+    L = self.L
+    if not getattr(L, "_bu_bound", False):
+        L.gtd_bottom_up.argtypes = [_vp, _vp, _i, _vp, _vp, _vp]
+        L._bu_bound = True
+    adj = np.ascontiguousarray(g.adj64(), dtype=np.uint64)
+    td = ctypes.c_int32()
+    par = np.zeros(g.n, dtype=np.int32)
+    order = np.zeros(g.n, dtype=np.int32)
+    self._check(L.gtd_bottom_up(self._h, _ptr(adj), g.n, ctypes.byref(td), _ptr(par), _ptr(order)))
+    return td.value, par, order
+
+
+Handle.bottom_up = _bottom_up
+
+
 def heuristic(g, kind: int = 0, scores=None):
     """Greedy incumbent (gtd_heuristic): kind 0 HighestDegree(Variance),
     1 HighestDegree, 2 Variance, 3 highest score first. Host only."""

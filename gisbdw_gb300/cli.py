@@ -9,10 +9,12 @@ values as strings like Boost's property-tree writer) and <that>.gviz (the
 elimination tree as an undirected graphviz graph, like boost::write_graphviz).
 
 Algorithms: dynGPU (exact subset DP, n <= 36), bnbGPU (exact branch and
-bound, connected graphs, n <= 104), highestDegreeHeur, varianceHeur and
-hdVarianceHeur (the greedy heuristics, host). The reference's CPU solvers
-(dynCPU, dynCPUImprov, bnbCPU) and the spanning-tree / bottom-up heuristics
-are not part of this library; naming them is an error.
+bound, connected graphs, n <= 104, seeded by the reference's bnbGPU chain
+HighestDegree(Variance(BottomUp))), highestDegreeHeur, varianceHeur and
+hdVarianceHeur (the greedy heuristics, host) and bottomUpHeur (the bottom-up
+union-find heuristic DP, GPU, n <= 32). The reference's CPU solvers (dynCPU,
+dynCPUImprov, bnbCPU) and the spanning-tree heuristic are not part of this
+library; naming them is an error.
 """
 from __future__ import annotations
 
@@ -29,8 +31,8 @@ import numpy as np
 from . import _lib
 from .graphs import Graph, from_text
 
-ALGORITHMS = ("dynGPU", "bnbGPU", "highestDegreeHeur", "varianceHeur", "hdVarianceHeur")
-NOT_PROVIDED = ("dynCPU", "dynCPUImprov", "bnbCPU", "spanningTreeHeur", "bottomUpHeur")
+ALGORITHMS = ("dynGPU", "bnbGPU", "highestDegreeHeur", "varianceHeur", "hdVarianceHeur", "bottomUpHeur")
+NOT_PROVIDED = ("dynCPU", "dynCPUImprov", "bnbCPU", "spanningTreeHeur")
 _HEURISTIC_KIND = {"hdVarianceHeur": 0, "highestDegreeHeur": 1, "varianceHeur": 2}
 
 
@@ -69,8 +71,12 @@ def solve(algorithm: str, g: Graph, handle=None):
     if algorithm == "dynGPU":
         td, parent, _, _ = handle.dp_solve(g.adj64(), g.n, want_order=False)
         return td, parent
+    if algorithm == "bottomUpHeur":
+        td, parent, _ = handle.bottom_up(g)
+        return td, parent
     if algorithm == "bnbGPU":
-        res = handle.bnb_solve_batch([g])
+        from .treedepth import reference_chain
+        res = handle.bnb_solve_batch([g], seeds=[reference_chain(handle, g)])
         if res["status"][0] != 0:
             raise _lib.DeadlineExceeded(int(res["status"][0]), "branch and bound deadline reached")
         return int(res["td"][0]), res["parents"][0]

@@ -299,6 +299,7 @@ gtd_status gtd_destroy(gtd_handle h) {
     cudaFree(h->d_btd);
     cudaFree(h->d_bparent);
     cudaFree(h->d_scratch);
+    cudaFree(h->d_bu);
     if (h->h_pinned)
       cudaFreeHost(h->h_pinned);
     if (h->h_bstage)

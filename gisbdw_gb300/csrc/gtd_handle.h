@@ -84,6 +84,8 @@ struct gtd_handle_s {
   gtd_bnb_state* bnb = nullptr;
   void* d_scratch = nullptr;  // general device scratch (labels, GNN batches)
   size_t scratch_cap = 0;
+  uint8_t* d_bu = nullptr;    // bottom-up heuristic: forests, heights, history
+  size_t bu_cap = 0;
 
   // Last DP solve (for gtd_dp_query / gtd_sync).
   bool have_table = false;

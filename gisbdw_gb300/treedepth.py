@@ -154,6 +154,25 @@ class BnBGPU:
         return Result(int(self._res["td"][0]), int(np.flatnonzero(par == -1)[0]), par.copy())
 
 
+def reference_chain(handle: _lib.Handle, g: Graph) -> Tuple[int, np.ndarray]:
+    """The incumbent chain of the reference's bnbGPU (main.cpp:178-186):
+    HighestDegree(Variance(BottomUpGPU)). Each heuristic returns its inner
+    heuristic's result when that is strictly lower, else its own
+    (highest_degree_heuristic.hpp:37-42); the bottom-up heuristic gives no
+    result beyond n = 32 (the reference's Get returns its UINT_MAX sentinel
+    when its DP cannot run to the end, bottom_up_heuristic.hpp:24-32).
+    Returns (td, parent)."""
+    best = (NO_RESULT, None)
+    if 1 <= g.n <= _lib.BOTTOM_UP_MAX_N:
+        td, par, _ = handle.bottom_up(g)
+        best = (td, par)
+    for kind in (2, 1):  # Variance, then HighestDegree around it
+        td, par = _lib.heuristic(g, kind)
+        if not best[0] < td:
+            best = (td, par)
+    return best
+
+
 def solve_exact(handle: _lib.Handle, graphs, dp_max_n: int = 28, deadline_ns: int = 0, guidance=None,
                 **bnb_kw) -> dict:
     """Exact treedepth of many connected graphs, each by the solver that suits

@@ -267,6 +267,25 @@ gtd_status gtd_heuristic(const uint64_t* adj2, int n, int kind,
                          const float* scores, int32_t* td_out,
                          int32_t* parent_out);
 
+/* Largest n of gtd_bottom_up (one 32-byte forest row per subset). */
+#define GTD_BOTTOM_UP_MAX_N 32
+
+/* BottomUpHeuristicGPU (src/branch_and_bound/heuristics/bottom_up_heuristic.hpp:
+ * 18-33 with its DP, bottom_up_heuristic_gpu_algorithm.cu:57-258), the
+ * innermost incumbent heuristic of the reference's bnbGPU / bnbCPU chains
+ * (main.cpp:170-186): level by level over all 2^n subsets, each subset keeps
+ * one elimination forest, that of a child S - v with v added as the root of
+ * its neighbours' trees, for the first v with the least height; the order of
+ * last-added vertices from V down (GetElimination) is replayed into an
+ * elimination tree. Host pointers: adj[n] in, td_out (the tree's height),
+ * parent_out[n] and, if non-null, order_out[n] out. Needs 2^n + 66 C(n, n/2)
+ * bytes of device memory (about 44 GB at n = 32). n > GTD_BOTTOM_UP_MAX_N
+ * gives GTD_NO_RESULT, as the reference's Get returns its no-result sentinel
+ * when the DP cannot run to the end (bottom_up_heuristic.hpp:24-32). */
+gtd_status gtd_bottom_up(gtd_handle h, const uint64_t* adj, int n,
+                         int32_t* td_out, int32_t* parent_out,
+                         int32_t* order_out);
+
 /* The same heuristics for many graphs in one GPU launch (one warp per
  * graph, n <= 128), trees identical to gtd_heuristic's: descs and the
  * (lo, hi) adjacency pool as for gtd_bnb_solve_batch; kind 0..3 as above

@@ -462,6 +462,127 @@ int gtdo_elimination_tree(int n, const uint64_t* adj, const int* order,
   return 0;
 }
 
+/* ---- BottomUpHeuristicGPU: bottom_up_heuristic_gpu_algorithm.cu ------ */
+
+/* ext_array_union_find::Find (ext_array_union_find.hpp:10-22): root of
+ * elem with path compression. Entries >= 0 are parents, a negative entry
+ * -v marks a root whose tree has value (height) v. */
+static int8_t uf_find(int8_t* uf, int8_t elem) {
+  int8_t root = elem;
+  while (uf[root] >= 0)
+    root = uf[root];
+  while (elem != root) {
+    int8_t prev = uf[elem];
+    uf[elem] = root;
+    elem = prev;
+  }
+  return root;
+}
+
+/* ext_array_union_find::Union (ext_array_union_find.hpp:24-33): s2's tree
+ * goes under s1, s1's value becomes max(own, value(s2) + 1), and the running
+ * maximum at val_ix follows it. */
+static void uf_union(int8_t* uf, int8_t s1, int8_t s2, int val_ix) {
+  if (s1 == s2)
+    return;
+  int8_t new_val = (int8_t)-uf[s1];
+  if (new_val <= -uf[s2])
+    new_val = (int8_t)(-uf[s2] + 1);
+  if (uf[val_ix] < new_val)
+    uf[val_ix] = new_val;
+  uf[s1] = (int8_t)-new_val;
+  uf[s2] = s1;
+}
+
+/* The bottom-up heuristic DP (Run :211-258, DynamicStepKernel :57-94): level
+ * i keeps one union-find forest per i-subset S (n + 2 entries: the forest,
+ * the last vertex added, the forest's height). S's forest is its child
+ * S \ s_j's forest with s_j added as the root over the trees of its
+ * neighbours in S, for the first j (ascending vertex) with the least height.
+ * GetElimination (bottom_up_heuristic_gpu_algorithm.hpp:104-120) then reads
+ * the last vertex of V, of V minus it, and so on: that order is order_out.
+ * Level 0: every entry -1, height 1 (:222-223). */
+int gtdo_bottom_up(int n, const uint64_t* adj, int* order_out) {
+  if (n < 1 || n > 30)
+    return -1;
+  const int W = n + 2;
+  uint64_t maxc = 0;
+  for (int k = 0; k <= n; ++k)
+    if (gtdo_nchoosek((uint64_t)n, (uint64_t)k) > maxc)
+      maxc = gtdo_nchoosek((uint64_t)n, (uint64_t)k);
+  int8_t* prev = (int8_t*)malloc((size_t)maxc * W);
+  int8_t* next = (int8_t*)malloc((size_t)maxc * W);
+  int8_t* last = (int8_t*)malloc(((size_t)1 << n) + 1); /* history: last vertex per (level, rank) */
+  uint64_t lvl_off[65];
+  if (!prev || !next || !last) {
+    free(prev);
+    free(next);
+    free(last);
+    return -2;
+  }
+  lvl_off[0] = 0;
+  for (int k = 0; k < n; ++k)
+    lvl_off[k + 1] = lvl_off[k] + gtdo_nchoosek((uint64_t)n, (uint64_t)k);
+  for (int j = 0; j < W; ++j)
+    prev[j] = -1;
+  prev[n + 1] = 1;
+  last[0] = -1;
+  int8_t uf[66];
+  int set[64];
+  for (int i = 1; i <= n; ++i) {
+    const uint64_t count = gtdo_nchoosek((uint64_t)n, (uint64_t)i);
+    for (uint64_t r = 0; r < count; ++r) {
+      gtdo_decode(n, i, r, set);
+      int8_t best = (int8_t)(i + 1);
+      int8_t* out = next + (size_t)r * W;
+      for (int j = 0; j < i; ++j) {
+        /* the child S \ s_j: its colex rank skips position j */
+        uint64_t code = 0;
+        for (int q = 0, pos = 0; q < i; ++q)
+          if (q != j)
+            code += gtdo_nchoosek((uint64_t)set[q], (uint64_t)(++pos));
+        memcpy(uf, prev + (size_t)code * W, (size_t)W);
+        const int v = set[j];
+        uf[n] = (int8_t)v;
+        for (uint64_t nb = adj[v]; nb; nb &= nb - 1) {
+          const int u = ctz64(nb);
+          int in = 0;
+          for (int q = 0; q < i; ++q)
+            in |= set[q] == u;
+          if (in)
+            uf_union(uf, (int8_t)v, uf_find(uf, (int8_t)u), n + 1);
+        }
+        if (uf[n + 1] < best) {
+          best = uf[n + 1];
+          memcpy(out, uf, (size_t)W);
+        }
+      }
+      last[lvl_off[i] + r] = out[n];
+    }
+    int8_t* t = prev;
+    prev = next;
+    next = t;
+  }
+  /* GetElimination(n, n, 0) */
+  int rem[64], k = n;
+  for (int v = 0; v < n; ++v)
+    rem[v] = v;
+  for (int step = 0; step < n; ++step) {
+    const uint64_t code = gtdo_encode(rem, k);
+    const int v = last[lvl_off[k] + code];
+    order_out[step] = v;
+    int w = 0;
+    for (int q = 0; q < k; ++q)
+      if (rem[q] != v)
+        rem[w++] = rem[q];
+    --k;
+  }
+  free(prev);
+  free(next);
+  free(last);
+  return 0;
+}
+
 /* ---- validity: common/utils/utils.hpp:50-86 ------------------------- */
 
 int gtdo_check_valid(int n, const uint64_t* adj, int td, const int* parent,

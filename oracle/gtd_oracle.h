@@ -73,6 +73,12 @@ int gtdo_dp_improv(int n, const uint64_t* adj, int* td, int* parent,
  * elimination_tree.hpp:193-215): eliminate order[0..n-1] in turn; each vertex
  * becomes a child of the vertex whose elimination created its component.
  * Returns 0, or -1 if order is not a permutation. */
+/* BottomUpHeuristicGPU's DP (bottom_up_heuristic_gpu_algorithm.cu:57-258)
+ * and its GetElimination order (n <= 30): order_out[n]. The heuristic's
+ * tree is the EliminationTree replay of that order (gtdo_elimination_tree),
+ * as BottomUpHeuristicGPU::Get does (bottom_up_heuristic.hpp:18-33). */
+int gtdo_bottom_up(int n, const uint64_t* adj, int* order_out);
+
 int gtdo_elimination_tree(int n, const uint64_t* adj, const int* order,
                           int* td, int* parent);
 

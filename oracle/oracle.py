@@ -65,6 +65,7 @@ class Port:
         L.gtdo_dp_solve.argtypes = [_i, _vp, _i, _ip, _vp]
         L.gtdo_dp_improv.argtypes = [_i, _vp, _ip, _vp, ctypes.POINTER(_i64)]
         L.gtdo_elimination_tree.argtypes = [_i, _vp, _vp, _ip, _vp]
+        L.gtdo_bottom_up.argtypes = [_i, _vp, _vp]
         L.gtdo_check_valid.argtypes = [_i, _vp, _i, _vp, _i]
         L.gtdo_heuristic.argtypes = [_i, _vp, _i, _ip, _vp]
         L.gtdo_bnb.argtypes = [_i, _vp, _i, _i, _i64, _ip, _vp, ctypes.POINTER(_i64)]
@@ -138,6 +139,18 @@ class Port:
         if rc:
             raise ValueError(f"gtdo_elimination_tree rc={rc}")
         return td.value, par
+
+    def bottom_up(self, g) -> Tuple[int, np.ndarray, List[int]]:
+        """BottomUpHeuristicGPU::Get (bottom_up_heuristic.hpp:18-33): the
+        bottom-up DP's elimination order and its EliminationTree replay:
+        (td, parent, order)."""
+        adj = g.adj64()
+        order = np.zeros(g.n, dtype=np.int32)
+        rc = self.L.gtdo_bottom_up(g.n, _ptr(adj), _ptr(order))
+        if rc:
+            raise ValueError(f"gtdo_bottom_up rc={rc}")
+        td, par = self.elimination_tree(g, order)
+        return td, par, order.tolist()
 
     def check_valid(self, g, td: int, parent, allow_forest: bool = False) -> bool:
         adj = g.adj64()

@@ -67,3 +67,16 @@ def test_exact_algorithms_match_oracle(tmp_path, port, algorithm):
     for g, path in zip(gs, paths):
         stats, _ = _read_outputs(path)
         assert int(stats["treedepth"]) == port.dp_solve(g)[0]
+
+
+@pytest.mark.gpu
+def test_bottom_up_heuristic_run_matches_oracle(tmp_path, port):
+    gs = [G.gnp_connected(15, 0.3, 4), G.grid(3, 5)]
+    srcs = [_write(tmp_path, g, f"b{i}") for i, g in enumerate(gs)]
+    out = tmp_path / "out"
+    out.mkdir()
+    paths = cli.run("bottomUpHeur", srcs, str(out), out=open(os.devnull, "w"))
+    for g, path in zip(gs, paths):
+        stats, _ = _read_outputs(path)
+        assert int(stats["treedepth"]) == port.bottom_up(g)[0]
+        assert stats["algorithmType"] == "bottomUpHeur"
