@@ -76,6 +76,11 @@ def parse_args():
     ap.add_argument("--cpu-bnb-sample", type=int, default=32, help="config-4 graphs in the CPU B&B baseline")
     ap.add_argument("--cpu-bnb-nodes", type=int, default=20_000_000,
                     help="search-node cap per graph of the CPU B&B baseline")
+    ap.add_argument("--c4-seeds", type=int, nargs="+", default=[4, 41, 42],
+                    help="config-4 graph sample seeds, one plain-vs-learned run each (spread over runs)")
+    ap.add_argument("--no-c5", action="store_true", help="skip the config-5 stream in the default line")
+    ap.add_argument("--c5-graphs", type=int, default=1024, help="graphs of the config-5 stream")
+    ap.add_argument("--c5-cap-s", type=float, default=60.0, help="per-graph cap of the config-5 stream")
     ap.add_argument("--bnb-memo-log2", type=int, default=0,
                     help="B&B memo slots per graph as a power of two (0 = sized from free HBM)")
     ap.add_argument("--label-graphs", type=int, default=10000,
@@ -317,7 +322,7 @@ def run_reference(args, graphs):
 # GPU arm.
 # ---------------------------------------------------------------------------
 
-def measure_dp_c3(h, steps, warmup, count=4096, device=0):
+def measure_dp_c3(h, steps, warmup, count=4096):
     """Batched uneven DP on config 3 (4096 graphs), device time from the
     library's events and host time of the whole C-ABI call."""
     import numpy as np
@@ -346,28 +351,17 @@ def measure_dp_c3(h, steps, warmup, count=4096, device=0):
         td, pars, st = h.dp_solve_batch(graphs, packed=packed)
         host.append(time.perf_counter() - t0)
         dev.append(st["dp_ms"])
-    # the same batch at every single tile size, and with each n at its own
-    # best size (mixed-size kernel, forced): what the plan chose against
+    # the same batch at every single tile size: what the plan chose against
     one_size = {}
     for lb in range(8, 13):
         h.dp_solve_batch(graphs, packed=packed, tile_bits=lb)
         one_size[str(lb)] = statistics.median(h.dp_solve_batch(graphs, packed=packed, tile_bits=lb)[2]["dp_ms"]
                                               for _ in range(max(3, steps // 2)))
-    per_n_best = {}
-    h2 = type(h)(device)
-    try:
-        h2.dp_set_rates(10, rates, mixed_eff=np.ones(5))  # efficiency 1: the per-n optimum, mixed
-        h2.dp_solve_batch(graphs, packed=packed)
-        runs = [h2.dp_solve_batch(graphs, packed=packed)[2] for _ in range(max(3, steps // 2))]
-        per_n_best = {"dp_ms": statistics.median(r["dp_ms"] for r in runs),
-                      "tile_bits_by_n": runs[-1]["tile_bits_by_n"]}
-    finally:
-        h2.close()
     peak, peak_kind = peaks()
     ms = statistics.median(dev)
     return {"graphs": len(graphs), "solves_per_s": len(graphs) / (ms / 1e3), "dp_ms": ms,
             "tile_bits_by_n": st["tile_bits_by_n"], "mixed_sizes": len(set(st["tile_bits_by_n"].values())) > 1,
-            "one_size_dp_ms": one_size, "per_n_best_mixed_kernel": per_n_best,
+            "one_size_dp_ms": one_size,
             "autotune_rates_subsets_per_us": {str(10 + i): [round(float(x), 1) for x in row]
                                               for i, row in enumerate(rates)},
             "autotune_mixed_kernel_efficiency": [round(float(x), 3) for x in mixed_eff],
@@ -380,14 +374,10 @@ def measure_dp_c3(h, steps, warmup, count=4096, device=0):
             "autotune_s": tune_s, "autotune_best_bits_n24": int(8 + rates[-1].argmax())}
 
 
-def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_nodes=0, family="c4"):
-    """Plain vs learned-guided B&B on the config 4 family (or the config 5
-    stream; identical graphs in both arms), the GNN trained here on DP
-    labels."""
-    import numpy as np
-    from gisbdw_gb300 import _lib, gnn
-    from gisbdw_gb300 import graphs as G
-    from gisbdw_gb300.validate import check_tree
+def train_guidance(h, n_label):
+    """The GNN trained on the GPU from exact DP labels (n <= 24 graphs of the
+    config-2/3 families); returns (net, info)."""
+    from gisbdw_gb300 import gnn
     base = gnn.training_graphs(n_label, seed=11)
     t0 = time.perf_counter()
     samples = gnn.label_set(h, base, per_graph=20, seed=1)
@@ -396,8 +386,20 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     net = gnn.GNN(h, seed=1)
     losses = gnn.train(net, train_set, epochs=4, batch_graphs=256, lr=3e-3)
     t2 = time.perf_counter()
-    acc = gnn.root_accuracy(net, test_set)
-    graphs = G.config4_graphs(count=n_graphs) if family == "c4" else G.config5_graphs(count=n_graphs)
+    info = {"labels": len(samples), "label_s": t1 - t0, "train_s": t2 - t1, "train_steps": len(losses),
+            "held_out": gnn.root_accuracy(net, test_set), "layers": gnn.LAYERS, "hidden": gnn.HIDDEN,
+            "weights": "bf16 (fp32 master, fp32 accumulation)"}
+    return net, info
+
+
+def bnb_arms(h, net, graphs, cap_s, memo_log2=0):
+    """Plain and learned-guided B&B on the same graphs: (summary, raw results).
+    Plain = ascending candidate order (the reference's DefaultAttemptOrder),
+    the reference heuristic chain's incumbent, top-down levels; learned = the
+    GNN's order, the better incumbent, its td estimate as the first level."""
+    import numpy as np
+    from gisbdw_gb300 import _lib, gnn
+    from gisbdw_gb300.validate import check_tree
     cap_ns = int(cap_s * 1e9)
     h.bnb_solve_batch(graphs[:4], deadline_ns=10**8, memo_log2=memo_log2)  # warm-up (allocation, module load)
     tp = time.perf_counter()
@@ -410,19 +412,24 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     t_inf = time.perf_counter() - t3
     learned = h.bnb_solve_batch(graphs, orders=gd["orders"], seeds=gd["seeds"], hints=gd["hints"],
                                 deadline_ns=cap_ns, memo_log2=memo_log2)
+    cap_ms = cap_s * 1e3
 
     def summary(res, extra_s=0.0):
         ok = res["status"] == 0
         pm = res["proof_ms"]
+        capped = np.where(ok, pm, cap_ms)
         fam = {}
         for f in ("rgg", "reg3", "grid", "tree"):
             sel = np.array([g.name.startswith(f) for g in graphs])
-            fam[f] = f"{int((ok & sel).sum())}/{int(sel.sum())}"
+            if sel.any():
+                fam[f] = f"{int((ok & sel).sum())}/{int(sel.sum())}"
+        gaps = (res["td"] - res["lower_bound"])[~ok]
         return {"solved": int(ok.sum()), "solves_per_s": float(ok.sum() / (res["stats"]["ms"] / 1e3)),
                 "e2e_solves_per_s": float(ok.sum() / (res["stats"]["total_ms"] / 1e3 + extra_s)),
                 "p50_proof_ms_solved": float(np.median(pm[ok])) if ok.any() else None,
-                "p50_proof_ms_capped": float(np.median(np.where(ok, pm, cap_s * 1e3))),
-                "p99_proof_ms_capped": float(np.percentile(np.where(ok, pm, cap_s * 1e3), 99)),
+                "p50_proof_ms_capped": float(np.median(capped)),
+                "p99_proof_ms_capped": float(np.percentile(capped, 99)),
+                "unproven_gap_td_minus_lb": np.bincount(gaps).tolist() if gaps.size else [],
                 "nodes": int(res["nodes"].sum()), "batch_ms": res["stats"]["ms"], "by_family": fam,
                 "nodes_per_s": float(res["nodes"].sum() / (res["stats"]["ms"] / 1e3)),
                 "p50_nodes_per_proven_graph": float(np.median(res["nodes"][ok])) if ok.any() else None,
@@ -435,16 +442,60 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
     both = (plain["status"] == 0) & (learned["status"] == 0)
     out = {"graphs": len(graphs), "cap_s": cap_s, "plain": ps, "learned": ls, "both_solved": int(both.sum()),
            "td_identical_on_both": bool(np.array_equal(plain["td"][both], learned["td"][both])),
-           "gnn": {"labels": len(samples), "label_s": t1 - t0, "train_s": t2 - t1, "train_steps": len(losses),
-                   "held_out": acc, "inference_s": t_inf, "plain_seed_s": t_seed,
-                   "layers": gnn.LAYERS, "hidden": gnn.HIDDEN,
-                   "weights": "bf16 (fp32 master, fp32 accumulation)"}}
+           "lower_bounds_consistent": bool(np.all(np.maximum(plain["lower_bound"], learned["lower_bound"]) <=
+                                                  np.minimum(plain["td"], learned["td"]))),
+           "p50_capped_plain_over_learned": ps["p50_proof_ms_capped"] / ls["p50_proof_ms_capped"],
+           "inference_s": t_inf, "plain_seed_s": t_seed}
     if both.any():
         pp, lp = np.median(plain["proof_ms"][both]), np.median(learned["proof_ms"][both])
         out["p50_proof_ms_both"] = {"plain": float(pp), "learned": float(lp), "plain_over_learned": float(pp / lp)}
+    return out, (plain, learned, gd)
+
+
+def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_nodes=0, family="c4",
+                seeds=(4,), net=None, gnn_info=None):
+    """Plain vs learned-guided B&B on the config 4 family (one run per graph
+    sample seed, identical graphs in both arms) or the config 5 stream, the
+    GNN trained here on DP labels."""
+    import numpy as np
+    from gisbdw_gb300 import graphs as G
+    from gisbdw_gb300.validate import check_tree
+    if net is None:
+        net, gnn_info = train_guidance(h, n_label)
+    runs = []
+    first = None
+    for seed in seeds:
+        graphs = G.config4_graphs(count=n_graphs, seed=seed) if family == "c4" else \
+            G.config5_graphs(count=n_graphs, seed=seed)
+        summ, raw = bnb_arms(h, net, graphs, cap_s, memo_log2)
+        summ["graph_seed"] = seed
+        runs.append(summ)
+        if first is None:
+            first = (graphs, raw)
+    out = dict(runs[0])
+    out["gnn"] = gnn_info
+    if len(runs) > 1:
+        def spread_of(vals):
+            vals = [v for v in vals if v is not None]
+            return {"min": min(vals), "median": statistics.median(vals), "max": max(vals)} if vals else None
+
+        def spread(key, arm=None):
+            return spread_of([(r[arm][key] if arm else r.get(key)) for r in runs])
+        out["runs"] = [{"graph_seed": r["graph_seed"], "plain_solved": r["plain"]["solved"],
+                        "learned_solved": r["learned"]["solved"], "both_solved": r["both_solved"],
+                        "p50_capped": [r["plain"]["p50_proof_ms_capped"], r["learned"]["p50_proof_ms_capped"]],
+                        "p99_capped": [r["plain"]["p99_proof_ms_capped"], r["learned"]["p99_proof_ms_capped"]],
+                        "p50_both_plain_over_learned": r.get("p50_proof_ms_both", {}).get("plain_over_learned"),
+                        "td_identical_on_both": r["td_identical_on_both"]} for r in runs]
+        out["spread"] = {"plain_solved": spread("solved", "plain"), "learned_solved": spread("solved", "learned"),
+                         "p50_both_plain_over_learned": spread_of(
+                             [x["p50_both_plain_over_learned"] for x in out["runs"]]),
+                         "p50_capped_plain_over_learned": spread("p50_capped_plain_over_learned")}
+    graphs, (plain, learned, gd) = first
     if family == "c5":
         # the same stream with the small graphs (n <= 28) given to the subset DP
         from gisbdw_gb300 import solve_exact
+        cap_ns = int(cap_s * 1e9)
         hy = solve_exact(h, graphs, dp_max_n=28, deadline_ns=cap_ns, guidance=gd, memo_log2=memo_log2)
         ok = hy["status"] == 0
         by_dp = np.array([s == "dp" for s in hy["solver"]])
@@ -470,7 +521,7 @@ def measure_bnb(h, n_graphs, cap_s, n_label, memo_log2=0, cpu_sample=0, cpu_node
             "sample": f"first {len(sample)} config-{family[1]} graphs; oracle restatement of BranchAndBound "
                       f"(branch_and_bound.cpp:51-114, EdgeLowerBound, HighestDegree(Variance)), "
                       f"{cpu_nodes} nodes per graph, {threads} host threads ({cpu_model()})"}
-    return out
+    return out, net, gnn_info
 
 
 def run_gpu(args, graphs):
@@ -596,10 +647,16 @@ def run_gpu(args, graphs):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_c3:
-        line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup, args.c3_graphs, local)
+        line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup, args.c3_graphs)
     if rank == 0 and not args.no_bnb:
-        line["bnb_c4"] = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
-                                     0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes)
+        line["bnb_c4"], net, gnn_info = measure_bnb(
+            h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
+            0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes,
+            seeds=tuple(args.c4_seeds))
+        if not args.no_c5:
+            line["bnb_c5"], _, _ = measure_bnb(h, args.c5_graphs, args.c5_cap_s, args.label_graphs,
+                                               args.bnb_memo_log2, family="c5", seeds=(5,), net=net,
+                                               gnn_info=gnn_info)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample = cpu_sample_graphs(graphs)
@@ -640,8 +697,9 @@ def run_bnb_stream(args):
     h = Handle(local)
     sampler = ClockSampler(local)
     sampler.start()
-    r = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
-                    0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes, family="c5")
+    r, _, _ = measure_bnb(h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
+                          0 if args.no_cpu_baseline else args.cpu_bnb_sample, args.cpu_bnb_nodes, family="c5",
+                          seeds=(5,))
     clocks = sampler.stop()
     L = r["learned"]
     line = {

@@ -463,8 +463,13 @@ def _bnb_method(self, graphs, orders=None, seeds=None, memo_log2: int = 0, deadl
                                       _ptr(status), _ptr(proof), _ptr(nodes), ctypes.byref(opts),
                                       ctypes.byref(stats)))
     parents = [par[d.offset:d.offset + d.n].copy() for d in descs]
+    lbs = np.zeros(count, dtype=np.int32)
+    if not getattr(L, "_lbs_bound", False):
+        L.gtd_bnb_lower_bounds.argtypes = [_vp, _vp, _i]
+        L._lbs_bound = True
+    self._check(L.gtd_bnb_lower_bounds(self._h, _ptr(lbs), count))
     return {"td": td, "parents": parents, "status": status, "proof_ms": proof, "nodes": nodes,
-            "stats": stats.as_dict(), "seed_td": seed_td}
+            "stats": stats.as_dict(), "seed_td": seed_td, "lower_bound": lbs}
 
 
 Handle.bnb_solve_batch = _bnb_method

@@ -42,13 +42,17 @@ constexpr int kLevelSlots = kDpMaxHigh + 2;
 
 // Tile bits per vertex count. An explicit opts->tile_bits gives every graph
 // that size. Otherwise, when the autotuner has rates (subsets per us of the
-// one-size kernel) for every n of the batch, the candidates are one size lb
-// for all graphs (predicted time sum 2^max(n, lb) / rate(n, lb)) and, per cap
-// c = 8..12, each n's own best size lb <= c run by the mixed-size kernel
-// (the same sum over the chosen sizes, divided by the mixed kernel's
-// measured efficiency at cap c); the least predicted time wins. No rates:
-// 10 bits. force_cap > 0 (the autotuner's own measurement) plans a mixed
-// launch at that cap.
+// one-size kernel at its own occupancy) for every n of the batch, the
+// candidates are
+//  * one size lb for all graphs: predicted time sum 2^max(n, lb) / rate(n, lb);
+//  * per cap c = 8..12, each n at its own best size lb <= c in the mixed-size
+//    kernel, whose shared memory is laid out for c: a size-lb tile then runs
+//    at the mixed kernel's occupancy at c instead of the one-size kernel's at
+//    lb (time x occ_one(lb) / occ_mixed(c) when that is above 1), divided by
+//    the autotuner's measured mixed-kernel efficiency at c with its own
+//    occupancy share taken out (what is left: the dispatch's extra work);
+// and the least predicted time wins. No rates: 10 bits. force_cap > 0 (the
+// autotuner's own measurement) plans a mixed launch at that cap.
 void pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const gtd_dp_batch_opts* opts, Plan& P,
                     int force_cap = 0) {
   std::vector<int> count_by_n(GTD_DP_MAX_N + 1, 0);
@@ -87,24 +91,35 @@ void pick_tile_bits(gtd_handle h, const gtd_graph_desc* descs, int count, const 
       uniform(lb);
     }
   }
+  int occ_one[kTuneLbMax + 1] = {};
+  for (int lb = kTuneLbMin; lb <= kTuneLbMax; ++lb)
+    occ_one[lb] = std::max(1, dp_tile_occupancy(lb));
   for (int c = kTuneLbMin; c <= kTuneLbMax; ++c) {
+    const int occ_mixed = dp_mixed_occupancy(c);
     const float eff = h->tune_mixed_eff[c];
-    if (eff <= 0)
+    if (eff <= 0 || occ_mixed < 1)
       continue;  // unmeasured: never mix at this cap
+    const double slow_c = std::max(1.0, double(occ_one[c]) / occ_mixed);
+    const double residual = std::min(1.0, eff * slow_c);  // efficiency beyond the occupancy effect
     int choice[GTD_DP_MAX_N + 1] = {};
     double cost = 0;
     int lo = kTuneLbMax, hi = kTuneLbMin;
     for (int n = 0; n <= GTD_DP_MAX_N; ++n) {
       if (!count_by_n[n])
         continue;
-      for (int lb = kTuneLbMin; lb <= c; ++lb)
-        if (!choice[n] || t_of(n, lb) < t_of(n, choice[n]))
+      double best_t = -1;
+      for (int lb = kTuneLbMin; lb <= c; ++lb) {
+        const double t = t_of(n, lb) * std::max(1.0, double(occ_one[lb]) / occ_mixed);
+        if (best_t < 0 || t < best_t) {
+          best_t = t;
           choice[n] = lb;
-      cost += t_of(n, choice[n]) * count_by_n[n];
+        }
+      }
+      cost += best_t * count_by_n[n];
       lo = std::min(lo, choice[n]);
       hi = std::max(hi, choice[n]);
     }
-    cost /= eff;
+    cost /= residual;
     if (lo != hi && hi == c && cost < best_cost) {
       best_cost = cost;
       P.lb = c;

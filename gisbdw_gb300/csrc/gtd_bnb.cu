@@ -1342,6 +1342,7 @@ struct gtd_bnb_state {
   size_t i8_cap = 0;
   uint8_t* mini = nullptr; // per-warp small-component DP tables
   size_t mini_cap = 0;
+  std::vector<int32_t> last_lb;  // proven lower bound per graph of the last solve
 };
 
 void gtd_bnb_release(gtd_handle h) {
@@ -1583,8 +1584,10 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   if (es != GTD_OK)
     return es;
   uint64_t total_nodes = 0;
+  B.last_lb.assign(count, 0);
   for (int i = 0; i < count; ++i) {
     const gtd_graph_desc& d = descs[i];
+    B.last_lb[i] = static_cast<int32_t>(std::min(lb[i], bst[i] >> 8));
     std::memcpy(parent_out + d.offset, par.data() + d.offset, d.n * sizeof(int32_t));
     const bool proved = lb[i] >= (bst[i] >> 8);
     status_out[i] = proved ? GTD_OK : GTD_TIMEOUT;
@@ -1601,5 +1604,16 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
     stats->nodes = total_nodes;
     stats->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t_call).count();
   }
+  return GTD_OK;
+}
+
+extern "C" gtd_status gtd_bnb_lower_bounds(gtd_handle h, int32_t* lb_out, int count) {
+  if (!h)
+    return GTD_INVALID_ARG;
+  if (!h->bnb || h->bnb->last_lb.empty())
+    return fail(h, GTD_NO_RESULT, "no branch-and-bound solve yet");
+  if (!lb_out || count != static_cast<int>(h->bnb->last_lb.size()))
+    return fail(h, GTD_INVALID_ARG, "count must be the last solve's batch size");
+  std::memcpy(lb_out, h->bnb->last_lb.data(), sizeof(int32_t) * count);
   return GTD_OK;
 }

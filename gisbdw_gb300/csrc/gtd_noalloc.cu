@@ -10,7 +10,7 @@
 //
 // So the scratch lives in one file-scope __device__ array of fixed size,
 // loaded with the library: every GPU that loads libgtd.so holds these
-// kNoallocScratchBytes (about 16.3 MiB) until the process exits. That bounds
+// kNoallocScratchBytes (about 16.1 MiB) until the process exits. That bounds
 // the graph size to n <= GTD_DP_NOALLOC_MAX_N (table 2^n bytes); larger n is
 // rejected with GTD_INVALID_ARG.
 //

@@ -258,6 +258,11 @@ gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* descs,
                                float* proof_ms_out, uint64_t* nodes_out,
                                const gtd_bnb_opts* opts, gtd_bnb_stats* stats);
 
+/* The proven lower bound on the treedepth of every graph of the last
+ * gtd_bnb_solve_batch call on h (count = that call's batch size): equal to
+ * td_out for proven graphs, below it for graphs whose deadline ran out. */
+gtd_status gtd_bnb_lower_bounds(gtd_handle h, int32_t* lb_out, int count);
+
 /* Greedy elimination heuristics (host only), the reference's incumbent
  * seeds (src/branch_and_bound/heuristics/): kind 0 HighestDegree(Variance)
  * (benchmark.cpp:50-55), 1 HighestDegree, 2 Variance, 3 highest score first
@@ -385,7 +390,7 @@ gtd_status gtd_gnn_make_labels(gtd_handle h, const uint64_t* adj2_pool,
  * a framework that owns all device memory). This entry point has no
  * counterpart in the reference. It allocates nothing: no handle, no
  * cudaMalloc/cudaFree. Its scratch is one fixed __device__ array of about
- * 16.3 MiB that every GPU loading this library holds until process exit, so
+ * 16.1 MiB that every GPU loading this library holds until process exit, so
  * it accepts 2 <= n <= GTD_DP_NOALLOC_MAX_N and rejects larger n with
  * GTD_INVALID_ARG. Inputs and outputs are DEVICE pointers owned by the
  * caller: adjacency d_adj[n]; outputs d_td (1 int), d_parent[n] and, if
