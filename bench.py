@@ -83,9 +83,10 @@ def parse_args():
     ap.add_argument("--c5-cap-s", type=float, default=60.0, help="per-graph cap of the config-5 stream")
     ap.add_argument("--bnb-memo-log2", type=int, default=0,
                     help="B&B memo slots per graph as a power of two (0 = sized from free HBM)")
-    ap.add_argument("--label-graphs", type=int, default=10000,
+    ap.add_argument("--label-graphs", type=int, default=10500,
                     help="graphs (n <= 24, config-2/3 families) whose DP tables label the GNN training set "
-                         "(each gives itself and 20 sampled subgraphs: ~200K labels at the default)")
+                         "(each gives itself and up to 20 distinct sampled subgraphs: ~201K labels at the "
+                         "default)")
     args = ap.parse_args()
     c5 = args.workload == "bnb-c5"
     if args.bnb_graphs is None:
@@ -431,6 +432,7 @@ def bnb_arms(h, net, graphs, cap_s, memo_log2=0):
                 "p99_proof_ms_capped": float(np.percentile(capped, 99)),
                 "unproven_gap_td_minus_lb": np.bincount(gaps).tolist() if gaps.size else [],
                 "nodes": int(res["nodes"].sum()), "batch_ms": res["stats"]["ms"], "by_family": fam,
+                "launches": 1, "passes": int(res["stats"].get("passes", 0)),
                 "nodes_per_s": float(res["nodes"].sum() / (res["stats"]["ms"] / 1e3)),
                 "p50_nodes_per_proven_graph": float(np.median(res["nodes"][ok])) if ok.any() else None,
                 "trees_valid": all(check_tree(g, int(t), par) for g, t, par in

@@ -338,7 +338,8 @@ class BnbOpts(ctypes.Structure):
 
 
 class BnbStats(ctypes.Structure):
-    _fields_ = [("ms", ctypes.c_float), ("total_ms", ctypes.c_float), ("nodes", ctypes.c_uint64)]
+    _fields_ = [("ms", ctypes.c_float), ("total_ms", ctypes.c_float), ("nodes", ctypes.c_uint64),
+                ("passes", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -32,13 +32,15 @@
 //    per-warp table (their exact td goes to the memo); the memo bounds of
 //    the vertex-deleted subsets C - v refute (td(C) >= td(C - v)) or accept
 //    (root v) a component before any root is tried.
-//  * Schedule: persistent launches over a global atomic queue of items
-//    (graph, level k, root candidate), issued for k descending from the
-//    incumbent minus one, candidates in priority order, graphs interleaved.
-//    Passes: an item may spend a node budget per launch; an item that spends
-//    it stops and is issued again in the next launch with twice its own
-//    budget (the memo keeps every subproblem it settled, so the rerun
-//    resumes cheaply). Only a window of W levels per graph runs at a time:
+//  * Schedule: one persistent cooperative launch over a global atomic queue
+//    of items (graph, level k, root candidate), issued for k descending from
+//    the incumbent minus one, candidates in priority order, graphs
+//    interleaved. Passes: an item may spend a node budget per pass; an item
+//    that spends it stops and is issued again in the next pass with twice
+//    its own budget (the memo keeps every subproblem it settled, so the
+//    rerun resumes cheaply). The last warp to finish a pass counts the open
+//    graphs and starts the next pass (next_pass: a bounded grid-wide wait;
+//    every CTA is resident). Only a window of W levels per graph runs at a time:
 //    k in (top - W, top], top = best - 1, or a caller's level hint clamped
 //    into [proven lower bound, best - 1] (the learned td estimate: it orders
 //    which decisions run first and never prunes; a wrong hint only moves the
@@ -116,7 +118,10 @@ constexpr MiniOrder make_mini_order() {
 static __device__ const MiniOrder kMiniOrder = make_mini_order();
 constexpr int kUnknownUb = 127;
 constexpr int kIoUnfinished = 3;         // d_io word: items that spent their budget this round
-constexpr int kIoExited = 200;           // d_io word: warps that left the current pass
+constexpr int kIoExited = 200;           // d_io words: warps that left the current pass, items started in it
+constexpr int kIoPassDone = 202;         // d_io word: warps that finished the current pass
+constexpr int kIoPassGen = 203;          // d_io word: passes completed (released by the pass's last warp)
+constexpr int kIoPassStop = 204;         // d_io word: 1 when no further pass is needed
 constexpr uint64_t kFirstBudget = 1024;  // search nodes of an item's first run
 constexpr uint32_t kMaxDoublings = 30;   // an item's budget grows to at most 2^30 times the first
 constexpr uint32_t kItemDone = 0xFF;
@@ -157,6 +162,10 @@ struct BnbParams {
   uint32_t* exited = nullptr;      // [0] warps that found no ticket left, [1] items started (this pass)
   uint32_t drain_at = 0;           // running items yield once this many warps have left
   uint32_t full_at = 0;            // ... and at least this many items have started
+  uint32_t* pass_done = nullptr;   // warps that finished the current pass
+  uint32_t* pass_gen = nullptr;    // passes completed
+  uint32_t* pass_stop = nullptr;   // set by the last warp of a pass: the search is over
+  uint64_t pass_wait_ns = 0;       // bound on a warp's wait for the rest of its pass
   int8_t* lvl_parent = nullptr;    // per graph x level: tree (max_n entries, -1 root)
   int32_t* status = nullptr;       // per graph BnbStatus
   uint64_t* t_begin = nullptr;     // per graph: first item start (globaltimer ns)
@@ -1045,6 +1054,60 @@ __device__ __forceinline__ void check_proved(const BnbParams& p, int g) {
     atomicCAS(p.t_end + g, 0ull, static_cast<unsigned long long>(global_ns()));
 }
 
+// End of a pass for one warp. Every warp arrives; the last one (all items of
+// the pass are then finished) counts the graphs still open, resets the pass
+// counters, decides whether another pass is needed and releases the next
+// pass; the others wait for that release, bounded by p.pass_wait_ns (on
+// expiry the kernel records a timeout and every warp leaves). Returns true
+// when the warp should run another pass. The launch is cooperative, so every
+// CTA is resident and the wait always ends.
+__device__ bool next_pass(const BnbParams& p, uint32_t pass) {
+  const int lane = threadIdx.x & 31;
+  int last = 0;
+  if (lane == 0) {
+    __threadfence();  // this warp's item results before its arrival
+    const uint32_t arrived = atomicAdd(p.pass_done, 1u) + 1u;
+    last = arrived == gridDim.x * static_cast<uint32_t>(kBnbWarps);
+    if (last)
+      __threadfence();  // every arrival (and what preceded it) before the bookkeeping
+  }
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (last) {
+    uint32_t open = 0;
+    for (int g = lane; g < p.num_graphs; g += 32)
+      open += ld_relaxed_s32(p.status + g) != kBnbTimeout &&
+              ld_acquire_u32(p.lbp + g) < (ld_acquire_u32(p.best + g) >> 8);
+    open = __reduce_add_sync(0xffffffffu, open);
+    if (lane == 0) {
+      const bool stop = open == 0 || ld_relaxed_s32(p.error) != 0 || pass + 1 >= static_cast<uint32_t>(kMaxRounds);
+      *reinterpret_cast<volatile uint32_t*>(p.ticket) = 0u;
+      *reinterpret_cast<volatile uint32_t*>(p.unfinished) = 0u;
+      reinterpret_cast<volatile uint32_t*>(p.exited)[0] = 0u;
+      reinterpret_cast<volatile uint32_t*>(p.exited)[1] = 0u;
+      *reinterpret_cast<volatile uint32_t*>(p.pass_done) = 0u;
+      *reinterpret_cast<volatile uint32_t*>(p.pass_stop) = stop ? 1u : 0u;
+      __threadfence();
+      st_release_u32(p.pass_gen, pass + 1u);
+    }
+  } else if (lane == 0) {
+    const uint64_t deadline = global_ns() + p.pass_wait_ns;
+    unsigned sleep_ns = 64;
+    while (ld_acquire_u32(p.pass_gen) <= pass) {
+      if (global_ns() > deadline) {
+        raise_error(p.error, kDevWaitTimeout, static_cast<int32_t>(pass));
+        break;
+      }
+      __nanosleep(sleep_ns);
+      if (sleep_ns < 4096)
+        sleep_ns *= 2;
+    }
+  }
+  uint32_t go = 0;
+  if (lane == 0)
+    go = ld_acquire_u32(p.pass_gen) > pass && ld_acquire_u32(p.pass_stop) == 0u && ld_relaxed_s32(p.error) == 0;
+  return __shfl_sync(0xffffffffu, go, 0) != 0;
+}
+
 __global__ void __launch_bounds__(32 * kBnbWarps, 6) bnb_kernel(const __grid_constant__ BnbParams p) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1053,6 +1116,7 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 6) bnb_kernel(const __grid_con
   const uint32_t S = p.split ? static_cast<uint32_t>(p.max_n) : 1u;  // second roots per first root
   const uint32_t per_level = static_cast<uint32_t>(p.max_n) * S * static_cast<uint32_t>(p.num_graphs);
   const uint32_t total = per_level * static_cast<uint32_t>(p.levels);
+  for (uint32_t pass = 0;; ++pass) {
   for (;;) {
     uint32_t item = 0;
     if (lane == 0)
@@ -1194,6 +1258,9 @@ __global__ void __launch_bounds__(32 * kBnbWarps, 6) bnb_kernel(const __grid_con
       }
     }
     __syncwarp();
+  }
+  if (!next_pass(p, pass))
+    break;
   }
 }
 
@@ -1532,31 +1599,22 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   if ((s = grow(h, &B.mini, &B.mini_cap, size_t(ctas) * kBnbWarps * (size_t(1) << kMiniMax))) != GTD_OK) return s;
   p.mini = B.mini;
   p.full_at = static_cast<uint32_t>(ctas * kBnbWarps);
-  GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
-  // Rounds: every item may spend `budget` nodes per launch; the host stops
-  // when every graph is proven or past its deadline.
-  std::vector<uint32_t> rbest(count), rlbp(count);
-  std::vector<int32_t> rstat(count);
-  int32_t rio[4] = {0, 0, 0, 0};
+  // One cooperative launch runs every pass: each item may spend its node
+  // budget per pass (twice its last one after a yield), and the last warp of
+  // a pass starts the next one until every graph is proven or past its
+  // deadline (next_pass). Cooperative: every CTA is resident, so the warps
+  // waiting at the end of a pass never wait on a CTA that cannot run.
   p.budget = (opts && opts->first_budget) ? opts->first_budget : kFirstBudget;
-  for (int round = 0; round < kMaxRounds; ++round) {
-    GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoTicket, 0, sizeof(int32_t), h->stream));
-    GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoUnfinished, 0, sizeof(int32_t), h->stream));
-    GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoExited, 0, 2 * sizeof(int32_t), h->stream));
-    bnb_kernel<<<static_cast<int>(ctas), 32 * kBnbWarps, smem, h->stream>>>(p);
-    GTD_CUDA(h, cudaGetLastError());
-    GTD_CUDA(h, cudaMemcpyAsync(rio, h->d_io, sizeof(rio), cudaMemcpyDeviceToHost, h->stream));
-    GTD_CUDA(h, cudaMemcpyAsync(rbest.data(), d_best, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-    GTD_CUDA(h, cudaMemcpyAsync(rlbp.data(), d_lbp, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-    GTD_CUDA(h, cudaMemcpyAsync(rstat.data(), d_status, count * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
-    GTD_CUDA(h, cudaStreamSynchronize(h->stream));
-    if (rio[kIoError] != 0)
-      break;
-    int open = 0;
-    for (int i = 0; i < count; ++i)
-      open += rstat[i] != kBnbTimeout && rlbp[i] < (rbest[i] >> 8);
-    if (open == 0)
-      break;
+  p.pass_done = reinterpret_cast<uint32_t*>(h->d_io + kIoPassDone);
+  p.pass_gen = reinterpret_cast<uint32_t*>(h->d_io + kIoPassGen);
+  p.pass_stop = reinterpret_cast<uint32_t*>(h->d_io + kIoPassStop);
+  p.pass_wait_ns = p.deadline_ns + 30ull * 1000 * 1000 * 1000;
+  GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoExited, 0, 5 * sizeof(int32_t), h->stream));
+  GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  {
+    void* args[] = {&p};
+    GTD_CUDA(h, cudaLaunchCooperativeKernel(reinterpret_cast<void*>(bnb_kernel), dim3(static_cast<unsigned>(ctas)),
+                                            dim3(32 * kBnbWarps), args, smem, h->stream));
   }
   const int tree_ctas = std::min(4096, (count + kBnbWarps - 1) / kBnbWarps);
   bnb_tree_kernel<<<tree_ctas, 32 * kBnbWarps, 0, h->stream>>>(p);
@@ -1577,6 +1635,8 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
   GTD_CUDA(h, cudaMemcpyAsync(nd.data(), d_nodes, count * sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream));
   GTD_CUDA(h, cudaMemcpyAsync(&t_first, d_t0, sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream));
   GTD_CUDA(h, cudaMemcpyAsync(io, h->d_io, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  uint32_t passes = 0;
+  GTD_CUDA(h, cudaMemcpyAsync(&passes, h->d_io + kIoPassGen, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
   GTD_CUDA(h, cudaMemcpyAsync(par.data(), d_parent, size_t(pool_len) * sizeof(int32_t), cudaMemcpyDeviceToHost,
                               h->stream));
   GTD_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -1602,6 +1662,7 @@ extern "C" gtd_status gtd_bnb_solve_batch(gtd_handle h, const gtd_graph_desc* de
     cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
     stats->ms = ms;
     stats->nodes = total_nodes;
+    stats->passes = static_cast<int32_t>(passes);
     stats->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t_call).count();
   }
   return GTD_OK;

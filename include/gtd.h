@@ -230,11 +230,13 @@ typedef struct {
   float ms;             /* device time of search + reconstruction (events) */
   float total_ms;       /* whole call */
   uint64_t nodes;       /* search nodes over the batch */
+  int32_t passes;       /* budgeted passes the one persistent launch ran */
 } gtd_bnb_stats;
 
 /* BranchAndBound (Treedepth/src/branch_and_bound/branch_and_bound.cpp:51-114)
- * and BnBGPU (bnb_gpu.cu:264-380) over a batch of connected graphs in
- * persistent launches (passes of node-budgeted items; a batch too small to
+ * and BnBGPU (bnb_gpu.cu:264-380) over a batch of connected graphs in ONE
+ * persistent (cooperative) launch that runs passes of node-budgeted items
+ * until every graph is proven or past its deadline (a batch too small to
  * fill the GPU is split into first-root x second-root items, so a single
  * graph uses n^2 warps): exact treedepth AND an elimination tree per graph (the
  * reference's GPU B&B returns the treedepth only). Graph i has n = descs[i].n

@@ -140,6 +140,11 @@ def test_bnb_unproven_improvements_carry_valid_trees(handle):
     gs = G.config4_graphs(count=12)
     res = handle.bnb_solve_batch(gs, deadline_ns=2 * 10**9)
     assert np.all(res["td"] <= res["seed_td"])
+    # one persistent launch ran several budgeted passes; the proven lower
+    # bounds never exceed the trees found
+    assert res["stats"]["passes"] > 1
+    assert np.all(res["lower_bound"] <= res["td"])
+    assert np.all((res["lower_bound"] == res["td"]) == (res["status"] == 0))
     for g, t, par in zip(gs, res["td"], res["parents"]):
         assert check_tree(g, t, par), g.name
 
