@@ -67,6 +67,7 @@ def parse_args():
     ap.add_argument("--tile-bits", type=int, default=0,
                     help="DP tile bits (0 = the library's default)")
     ap.add_argument("--no-c3", action="store_true", help="skip the batched DP measurement")
+    ap.add_argument("--no-bottom-up", action="store_true", help="skip the bottom-up heuristic measurement")
     ap.add_argument("--c3-graphs", type=int, default=4096, help="graphs of the batched DP measurement (config 3)")
     ap.add_argument("--no-bnb", action="store_true", help="skip the plain vs learned B&B measurement")
     ap.add_argument("--bnb-graphs", type=int, default=None,
@@ -375,6 +376,42 @@ def measure_dp_c3(h, steps, warmup, count=4096):
             "autotune_s": tune_s, "autotune_best_bits_n24": int(8 + rates[-1].argmax())}
 
 
+def measure_bottom_up(h, cpu=1):
+    """The bottom-up union-find heuristic DP (gtd_bottom_up) on connected
+    G(n, 0.2) graphs: device time per graph, its algorithmic bytes (per
+    subset S: |S| child rows of 32 B and |S| child heights read, one 32-byte
+    row, a height and a history byte written) over that time, and the
+    oracle's restatement timed on one host thread at the smallest n with its
+    order compared."""
+    from gisbdw_gb300 import graphs as G
+    peak, peak_kind = peaks()
+    out = {"graphs": {}}
+    for n in (20, 26, 30):
+        g = G.gnp_connected(n, 0.2, 900 + n)
+        h.bottom_up(g)  # warm-up (allocation)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            td, par, order = h.bottom_up(g)
+            ts.append(time.perf_counter() - t0)
+        t = min(ts)
+        alg = (2 ** n) * (33 * n / 2 + 34)
+        out["graphs"][g.name] = {"n": n, "td": int(td), "ms": 1e3 * t, "alg_GBps": alg / t / 1e9,
+                                 "frac_of_" + peak_kind + "_hbm": alg / t / 1e9 / peak}
+        if cpu and n == 20:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            t0 = time.perf_counter()
+            otd, opar, oorder = oracle.Port().bottom_up(g)
+            cpu_s = time.perf_counter() - t0
+            out["cpu_baseline"] = {"graph": g.name, "value_ms": 1e3 * cpu_s, "cores": 1, "kind": "port",
+                                   "same_order_and_td": oorder == order.tolist() and otd == td,
+                                   "gpu_over_cpu_speedup": cpu_s / t}
+    out["note"] = "ms = whole gtd_bottom_up call (n launches + order + host replay); alg bytes per subset " \
+                  "(|S| (32 + 1) read + 34 written) over that time"
+    return out
+
+
 def train_guidance(h, n_label):
     """The GNN trained on the GPU from exact DP labels (n <= 24 graphs of the
     config-2/3 families); returns (net, info)."""
@@ -650,6 +687,8 @@ def run_gpu(args, graphs):
     }
     if rank == 0 and not args.no_c3:
         line["dp_c3"] = measure_dp_c3(h, args.steps, args.warmup, args.c3_graphs)
+    if rank == 0 and not args.no_bottom_up:
+        line["bottom_up"] = measure_bottom_up(h, 0 if args.no_cpu_baseline else 1)
     if rank == 0 and not args.no_bnb:
         line["bnb_c4"], net, gnn_info = measure_bnb(
             h, args.bnb_graphs, args.bnb_cap_s, args.label_graphs, args.bnb_memo_log2,
