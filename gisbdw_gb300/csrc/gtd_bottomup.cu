@@ -56,6 +56,12 @@ struct BuParams {
 };
 
 __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_constant__ BuParams p) {
+  // The binomial table in shared memory: lanes read different entries
+  // (C(lane, k)), which the parameter bank would serve one address at a time.
+  __shared__ uint32_t binom[kBuMaxN + 1][kBuMaxN + 1];
+  for (int i = threadIdx.x; i < (kBuMaxN + 1) * (kBuMaxN + 1); i += blockDim.x)
+    (&binom[0][0])[i] = (&p.binom[0][0])[i];
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const uint32_t full = 0xffffffffu;
   const uint64_t my_adj = lane < p.n ? p.adj[lane] : 0ull;
@@ -64,16 +70,16 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
     // unrank r among the i-subsets (colex): the largest a with C(a, k) <= rest
     uint32_t S = 0, rest = r;
     for (int k = p.level; k > 0; --k) {
-      const uint32_t c = lane < p.n ? p.binom[lane][k] : 0xffffffffu;
+      const uint32_t c = lane < p.n ? binom[lane][k] : 0xffffffffu;
       const int a = 31 - __clz(__ballot_sync(full, c <= rest));
       S |= 1u << a;
-      rest -= p.binom[a][k];
+      rest -= binom[a][k];
     }
     // lane v in S: colex rank of S - v (bits below v keep their term
     // C(u, q + 1), bits above shift down to C(u, q))
     const bool inS = (S >> lane) & 1u;
     const uint32_t q = __popc(S & ((1u << lane) - 1u));
-    const uint32_t t1 = inS ? p.binom[lane][q + 1] : 0u, t0 = inS ? p.binom[lane][q] : 0u;
+    const uint32_t t1 = inS ? binom[lane][q + 1] : 0u, t0 = inS ? binom[lane][q] : 0u;
     uint32_t pre = t1, suf = t0;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -88,11 +94,23 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
 
     uint32_t best = 0xffu, best_v = 0xffu;
     uint32_t best_ent = kFreshRoot;
-    for (uint32_t todo = S; todo; todo &= todo - 1) {  // candidates in ascending order
-      const int v = __ffs(todo) - 1;
-      const uint32_t c = __shfl_sync(full, child, v);
-      const uint32_t ent = lane < p.n ? p.prev[size_t(c) * 32 + lane] : kFreshRoot;
-      const uint32_t hc = p.prev_h[c];
+    // candidates in ascending order; the next candidate's child row is loaded
+    // while the current one is evaluated
+    uint32_t todo = S;
+    int v = __ffs(todo) - 1;
+    uint32_t c = __shfl_sync(full, child, v);
+    uint32_t ent = lane < p.n ? p.prev[size_t(c) * 32 + lane] : kFreshRoot;
+    uint32_t hc = p.prev_h[c];
+    for (;;) {
+      const uint32_t todo_next = todo & (todo - 1);
+      int v_next = 0;
+      uint32_t ent_next = kFreshRoot, hc_next = 0;
+      if (todo_next) {  // warp-uniform
+        v_next = __ffs(todo_next) - 1;
+        const uint32_t c_next = __shfl_sync(full, child, v_next);
+        ent_next = lane < p.n ? p.prev[size_t(c_next) * 32 + lane] : kFreshRoot;
+        hc_next = p.prev_h[c_next];
+      }
       const bool is_root = ent & 0x80u;
       const uint32_t root = is_root ? static_cast<uint32_t>(lane) : ent;
       const uint64_t nb = __shfl_sync(full, my_adj, v) & S;
@@ -104,6 +122,12 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
         best_v = static_cast<uint32_t>(v);
         best_ent = lane == v ? (0x80u | (m + 1)) : (((R >> root) & 1u) ? static_cast<uint32_t>(v) : ent);
       }
+      if (!todo_next)
+        break;
+      todo = todo_next;
+      v = v_next;
+      ent = ent_next;
+      hc = hc_next;
     }
     p.next[size_t(r) * 32 + lane] = static_cast<uint8_t>(best_ent);
     if (lane == 0) {
