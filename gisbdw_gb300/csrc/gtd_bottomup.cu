@@ -64,7 +64,8 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const uint32_t full = 0xffffffffu;
-  const uint64_t my_adj = lane < p.n ? p.adj[lane] : 0ull;
+  // lane u's neighbours (n <= 32); u is a neighbour of v iff v is one of u's
+  const uint32_t my_adj = lane < p.n ? static_cast<uint32_t>(p.adj[lane]) : 0u;
   const uint32_t warps = gridDim.x * kBuWarps;
   for (uint32_t r = blockIdx.x * kBuWarps + (threadIdx.x >> 5); r < p.count; r += warps) {
     // unrank r among the i-subsets (colex): the largest a with C(a, k) <= rest
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
     uint32_t todo = S;
     int v = __ffs(todo) - 1;
     uint32_t c = __shfl_sync(full, child, v);
-    uint32_t ent = lane < p.n ? p.prev[size_t(c) * 32 + lane] : kFreshRoot;
+    uint32_t ent = p.prev[size_t(c) * 32 + lane];  // rows are whole: lanes >= n hold fresh roots
     uint32_t hc = p.prev_h[c];
     for (;;) {
       const uint32_t todo_next = todo & (todo - 1);
@@ -108,13 +109,13 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
       if (todo_next) {  // warp-uniform
         v_next = __ffs(todo_next) - 1;
         const uint32_t c_next = __shfl_sync(full, child, v_next);
-        ent_next = lane < p.n ? p.prev[size_t(c_next) * 32 + lane] : kFreshRoot;
+        ent_next = p.prev[size_t(c_next) * 32 + lane];
         hc_next = p.prev_h[c_next];
       }
       const bool is_root = ent & 0x80u;
       const uint32_t root = is_root ? static_cast<uint32_t>(lane) : ent;
-      const uint64_t nb = __shfl_sync(full, my_adj, v) & S;
-      const uint32_t R = __reduce_or_sync(full, ((nb >> lane) & 1ull) ? (1u << root) : 0u);
+      const bool nbr = inS && ((my_adj >> v) & 1u);  // lane is a neighbour of v inside S
+      const uint32_t R = __reduce_or_sync(full, nbr ? (1u << root) : 0u);
       const uint32_t m = __reduce_max_sync(full, ((R >> lane) & 1u) ? (ent & 0x7Fu) : 0u);
       const uint32_t h = max(hc, m + 1);
       if (h < best) {  // strict: the first v with the least height
