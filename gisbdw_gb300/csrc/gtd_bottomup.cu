@@ -39,6 +39,7 @@ namespace {
 
 constexpr int kBuMaxN = GTD_BOTTOM_UP_MAX_N;  // 32: one 32-byte row, lane = vertex
 constexpr int kBuWarps = 8;
+constexpr int kBuChunk = 16;  // consecutive subsets per warp between unrankings
 constexpr uint8_t kFreshRoot = 0x81;  // a root of height 1 (a vertex not yet added)
 
 struct BuParams {
@@ -67,14 +68,26 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
   // lane u's neighbours (n <= 32); u is a neighbour of v iff v is one of u's
   const uint32_t my_adj = lane < p.n ? static_cast<uint32_t>(p.adj[lane]) : 0u;
   const uint32_t warps = gridDim.x * kBuWarps;
-  for (uint32_t r = blockIdx.x * kBuWarps + (threadIdx.x >> 5); r < p.count; r += warps) {
-    // unrank r among the i-subsets (colex): the largest a with C(a, k) <= rest
-    uint32_t S = 0, rest = r;
-    for (int k = p.level; k > 0; --k) {
-      const uint32_t c = lane < p.n ? binom[lane][k] : 0xffffffffu;
-      const int a = 31 - __clz(__ballot_sync(full, c <= rest));
-      S |= 1u << a;
-      rest -= binom[a][k];
+  // Each warp takes kBuChunk consecutive ranks: it unranks the first and
+  // steps to the next subset of the level in colex order (the next larger
+  // mask of the same popcount) for the others.
+  uint32_t S = 0;
+  for (uint64_t r = uint64_t(blockIdx.x * kBuWarps + (threadIdx.x >> 5)) * kBuChunk, first = r, cend = 0;
+       r < p.count; ++r) {
+    if (r == first) {
+      cend = first + kBuChunk;
+      // unrank r among the i-subsets (colex): the largest a with C(a, k) <= rest
+      uint32_t rest = static_cast<uint32_t>(r);
+      S = 0;
+      for (int k = p.level; k > 0; --k) {
+        const uint32_t c = lane < p.n ? binom[lane][k] : 0xffffffffu;
+        const int a = 31 - __clz(__ballot_sync(full, c <= rest));
+        S |= 1u << a;
+        rest -= binom[a][k];
+      }
+    } else {
+      const uint64_t low = S & (0u - S), up = uint64_t(S) + low;  // warp-uniform
+      S = static_cast<uint32_t>(((up ^ S) >> (__ffs(static_cast<int>(S)) + 1)) | up);
     }
     // lane v in S: colex rank of S - v (bits below v keep their term
     // C(u, q + 1), bits above shift down to C(u, q))
@@ -134,6 +147,10 @@ __global__ void __launch_bounds__(32 * kBuWarps) bu_level_kernel(const __grid_co
     if (lane == 0) {
       p.next_h[r] = static_cast<uint8_t>(best);
       p.last[p.last_off + r] = static_cast<uint8_t>(best_v);
+    }
+    if (r + 1 == cend) {  // chunk done: jump to this warp's next chunk
+      first = r + 1 + uint64_t(warps - 1) * kBuChunk;
+      r = first - 1;
     }
   }
 }
@@ -262,7 +279,7 @@ extern "C" gtd_status gtd_bottom_up(gtd_handle h, const uint64_t* adj, int n, in
     p.prev_h = h_a;
     p.next = rows_b;
     p.next_h = h_b;
-    const uint64_t ctas = std::min<uint64_t>(max_ctas, (p.count + kBuWarps - 1) / kBuWarps);
+    const uint64_t ctas = std::min<uint64_t>(max_ctas, (p.count + kBuWarps * kBuChunk - 1) / (kBuWarps * kBuChunk));
     bu_level_kernel<<<static_cast<unsigned>(ctas), 32 * kBuWarps, 0, h->stream>>>(p);
     GTD_CUDA(h, cudaGetLastError());
     std::swap(rows_a, rows_b);
