@@ -6,16 +6,23 @@ Workload (default, ``--workload dp-c2``): the single-graph subset DP at scale,
 elimination tree). The DP tables (256 MiB - 4 GiB) are larger than L2, so no
 flush is needed between steps.
 
-The same line carries two more measurements of the run:
-  dp_c3   batched uneven DP, 4096 graphs n in [10, 24] (three families), one
-          persistent launch per step replayed from a CUDA graph;
-  bnb_c4  plain vs learned-guided GPU branch and bound on 256 sparse graphs
-          n in [40, 64] (random geometric, random 3-regular, deleted grids)
-          with a per-graph cap: plain = ascending candidate order (the
-          reference's DefaultAttemptOrder) and the reference heuristic's
-          incumbent; learned = the GNN's score order and the better of that
-          incumbent and a score-greedy elimination. The GNN is trained in the
-          run, on the GPU, from labels the GPU DP computes.
+The same line carries more measurements of the run:
+  dp_c3      batched uneven DP, 4096 graphs n in [10, 24] (three families), one
+             persistent launch per step replayed from a CUDA graph, tile sizes
+             per vertex count planned from the autotuner's rates;
+  bottom_up  the bottom-up union-find heuristic DP at n = 20 / 26 / 30, and the
+             oracle's restatement on one host thread at n = 20;
+  bnb_c4     plain vs learned-guided GPU branch and bound on 256 sparse graphs
+             n in [40, 64] (random geometric, random 3-regular, deleted grids)
+             with a 10 s per-graph cap, on three graph samples: plain =
+             ascending candidate order (the reference's DefaultAttemptOrder)
+             and the reference heuristic's incumbent; learned = the GNN's score
+             order, the better of that incumbent and a score-greedy
+             elimination, and its td estimate as the first level. The GNN is
+             trained in the run, on the GPU, from ~201 K labels the GPU DP
+             computes;
+  bnb_c5     the config-5 stream (1024 graphs, n in [20, 80], 60 s cap), the
+             same arms, plus the size-dispatch hybrid.
 
 Arms:
   default            gtd on the GPU; ``value`` = solves/s with inputs resident
