@@ -109,3 +109,31 @@ def test_abort_stops_a_running_search_and_handle_recovers(fresh):
     assert out["s"] < 20, out
     res = fresh.bnb_solve_batch([G.cycle(9)], deadline_ns=10**10)
     assert res["status"][0] == 0 and res["td"][0] == 5
+
+
+def test_abort_stops_a_waiting_dp_solve(fresh):
+    """A DP solve whose first tile is never taken (the injected stall) would
+    wait 30 s for its dependencies; gtd_abort from another thread ends it with
+    GTD_ABORTED within seconds, and the next solve is exact."""
+    g = G.gnp_connected(22, 0.25, 6)
+    out = {}
+
+    def run():
+        t0 = time.perf_counter()
+        try:
+            fresh.dp_solve(g.adj64(), g.n, timeout_ns=30 * 10**9)
+            out["status"] = 0
+        except _lib.GtdError as e:
+            out["status"] = e.status
+        out["s"] = time.perf_counter() - t0
+
+    _lib.inject_fault(_lib.FAULT_STALL, 1)
+    th = threading.Thread(target=run)
+    th.start()
+    time.sleep(1.0)
+    fresh.abort()
+    th.join(timeout=60)
+    assert not th.is_alive()
+    assert out["status"] == 5 and out["s"] < 10, out  # GTD_ABORTED
+    td, _, _, _ = fresh.dp_solve(g.adj64(), g.n)
+    assert td == fresh.dp_solve(g.adj64(), g.n, tile_bits=8)[0]
