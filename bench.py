@@ -69,6 +69,9 @@ def parse_args():
     ap.add_argument("--workload", default="dp-c2", choices=["dp-c2", "bnb-c5"],
                     help="dp-c2: the default line; bnb-c5: the config-5 B&B stream")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--partition", action="store_true",
+                    help="N > 1: split the workload's graphs over the ranks, size-balanced (strong scaling) "
+                         "instead of every rank solving all of them (replicas, weak scaling)")
     ap.add_argument("--only-n", type=int, default=0,
                     help="restrict the workload to its graphs with this n (profiling)")
     ap.add_argument("--tile-bits", type=int, default=0,
@@ -122,6 +125,35 @@ def job_rate(units_per_rank, elapsed_s, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_s = float(t.item())
     return units_per_rank * world / elapsed_s, elapsed_s
+
+
+def partition_graphs(graphs, world):
+    """Size-balanced split of a graph list over `world` ranks (longest first
+    to the least-loaded rank; the cost of a DP solve is 2^n): rank r solves
+    the graphs at the indices parts[r]. Deterministic, so every rank computes
+    the same split without communicating."""
+    loads = [0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(graphs)), key=lambda i: (-graphs[i].n, i)):
+        r = min(range(world), key=lambda r: (loads[r], r))
+        parts[r].append(i)
+        loads[r] += 2 ** graphs[i].n
+    return [sorted(p) for p in parts]
+
+
+def job_rate_total(units, elapsed_s, world):
+    """Whole-job throughput when the ranks share one workload: the sum of
+    the ranks' units over the slowest rank's time (all-reduces of the
+    process group when world > 1). Returns (rate, slowest elapsed seconds)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(elapsed_s)], dtype=torch.float64)
+        u = torch.tensor([float(units)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        elapsed_s, units = float(t.item()), float(u.item())
+    return units / elapsed_s, elapsed_s
 
 
 def peaks():
@@ -582,6 +614,12 @@ def run_gpu(args, graphs):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
+    all_graphs = graphs
+    partitioned = world > 1 and args.partition
+    if partitioned:
+        if world > len(all_graphs):
+            raise SystemExit(f"--partition needs at most {len(all_graphs)} ranks")
+        graphs = [all_graphs[i] for i in partition_graphs(all_graphs, world)[rank]]
     # The library runs on this torch stream, so the CUDA events below bracket
     # its kernels on the stream they are launched on.
     stream = torch.cuda.Stream()
@@ -628,7 +666,8 @@ def run_gpu(args, graphs):
     barrier()
     elapsed_ms = ev0.elapsed_time(ev1)
     clocks = sampler.stop()
-    value, elapsed_s = job_rate(len(graphs) * args.steps, elapsed_ms / 1000.0, world)
+    rate = job_rate_total if partitioned else job_rate
+    value, elapsed_s = rate(len(graphs) * args.steps, elapsed_ms / 1000.0, world)
     elapsed_ms = elapsed_s * 1000.0
 
     # e2e: host buffers through the C ABI call (adjacency H2D, results D2H)
@@ -646,7 +685,7 @@ def run_gpu(args, graphs):
             gpu_out[g.name] = h.dp_solve(adjs[i], g.n, tile_bits=args.tile_bits)[:3]
     e2e_s = time.perf_counter() - t0
     barrier()
-    e2e_value, _ = job_rate(len(graphs) * args.steps, e2e_s, world)
+    e2e_value, _ = rate(len(graphs) * args.steps, e2e_s, world)
 
     # roofline of the dominant kernel (dp_tile_kernel), from live events
     alg = sum(s["alg_bytes"] for s in kstats)
@@ -668,9 +707,11 @@ def run_gpu(args, graphs):
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-        "data": "synthetic",
-        "config": config_c2(graphs), "parallelism": "replicas" if world > 1 else "1 GPU",
+        "higher_is_better": True, "scaling": "strong" if partitioned else "weak", "vs_baseline": None,
+        "dtype": "u8", "data": "synthetic",
+        "config": config_c2(all_graphs),
+        "parallelism": (f"graphs partitioned over {world} ranks" if partitioned else
+                        "replicas" if world > 1 else "1 GPU"),
         "p50_time_to_proof_ms": statistics.median(per_graph_ms),
         "treedepths": tds,
         "roofline": {"bound": "hbm", "kernel": "dp_tile_kernel", "achieved": achieved, "peak": peak,
@@ -705,7 +746,7 @@ def run_gpu(args, graphs):
             line["bnb_c5"], _, _ = measure_bnb(h, args.c5_graphs, args.c5_cap_s, args.label_graphs,
                                                args.bnb_memo_log2, family="c5", seeds=(5,), net=net,
                                                gnn_info=gnn_info)
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sample = cpu_sample_graphs(graphs)
         res = time_cpu_dp(sample, len(sample), threads)
