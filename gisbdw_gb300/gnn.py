@@ -407,6 +407,97 @@ def training_graphs(count: int, seed: int = 11) -> List[Graph]:
     return out
 
 
+def family_graphs(count: int, seed: int = 13, n_min: int = 26, n_max: int = 32) -> List[Graph]:
+    """Larger label base graphs of the sparse B&B families (random geometric,
+    random 3-regular, deleted grids, trees plus extra edges), n in
+    [n_min, n_max] — still inside the subset DP's exact range — drawn with
+    seeds of their own (70000 + ...), apart from the benchmark graphs."""
+    from . import graphs as G
+    out = []
+    for i in range(count):
+        n = n_min + (i * 5 + seed) % (n_max - n_min + 1)
+        s = 70000 + 31 * seed + i
+        fam = i % 4
+        if fam == 0:
+            out.append(G.random_geometric(n, 3.0 + (i % 5) * 0.5, s))
+        elif fam == 1:
+            out.append(G.random_regular3(n - (n % 2), s))
+        elif fam == 2:
+            out.append(G.grid_deleted(n, 0.1, s))
+        else:
+            out.append(G.tree_plus_edges(n, (i * 3) % (n // 2 + 1), s))
+    return out
+
+
+def _grow_subset(g: Graph, size: int, rng: np.random.Generator) -> List[int]:
+    """A connected vertex set of `size` vertices grown from a random vertex
+    by random frontier vertices (fewer when its component is smaller)."""
+    adj = g.adjacency_masks()
+    start = int(rng.integers(g.n))
+    chosen, frontier = 1 << start, adj[start] & ~(1 << start)
+    while bin(chosen).count("1") < size and frontier:
+        cand = [v for v in range(g.n) if frontier >> v & 1]
+        v = cand[int(rng.integers(len(cand)))]
+        chosen |= 1 << v
+        frontier = (frontier | adj[v]) & ~chosen
+    return [v for v in range(g.n) if chosen >> v & 1]
+
+
+def family_label_set(handle: _lib.Handle, graphs: Sequence[Graph], per_graph: int, seed: int = 0,
+                     drop: int = 12) -> "LabelSet":
+    """Labels at larger sizes (n <= 36): every graph is solved exactly by the
+    GPU subset DP; the graph itself and `per_graph` connected induced
+    subgraphs of it (sizes uniform in [n - drop, n]) are labelled from its
+    table with their treedepth and optimal-root mask (gtd_dp_labels),
+    relabelled 0..k-1 in vertex order."""
+    L = _bind(handle.L)
+    rng = np.random.default_rng(seed)
+    adj_parts, ns, roots_out, tds = [], [], [], []
+    for g in graphs:
+        handle.dp_solve(g.adj64(), g.n, want_order=False)
+        sets = [list(range(g.n))]
+        for _ in range(per_graph):
+            size = int(rng.integers(max(5, g.n - drop), g.n + 1))
+            sets.append(_grow_subset(g, size, rng))
+        masks = np.array([sum(1 << v for v in vs) for vs in sets], dtype=np.uint64)
+        td = np.zeros(len(sets), dtype=np.int32)
+        roots = np.zeros(len(sets), dtype=np.uint64)
+        handle._check(L.gtd_dp_labels(handle._h, _p(masks), len(sets), _p(td), _p(roots)))
+        A = np.zeros((g.n, g.n), dtype=np.uint64)
+        e = g.edge_array()
+        if e.size:
+            A[e[:, 0], e[:, 1]] = 1
+            A[e[:, 1], e[:, 0]] = 1
+        for vs, t, r in zip(sets, td.tolist(), roots.tolist()):
+            idx = np.asarray(vs, dtype=np.int64)
+            k = len(vs)
+            bits = np.left_shift(np.uint64(1), np.arange(k, dtype=np.uint64))
+            a2 = np.zeros(2 * k, dtype=np.uint64)
+            a2[0::2] = (A[np.ix_(idx, idx)] * bits).sum(axis=1, dtype=np.uint64)  # k <= 36 < 64 bits
+            rbits = (np.uint64(r) >> idx.astype(np.uint64)) & np.uint64(1)
+            adj_parts.append(a2)
+            ns.append(k)
+            roots_out.append(int((rbits * bits).sum(dtype=np.uint64)))
+            tds.append(t)
+    ns = np.array(ns, dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+    return LabelSet(np.concatenate(adj_parts), ns, offs, np.array(roots_out, dtype=np.uint64),
+                    np.array(tds, dtype=np.int32))
+
+
+def merge(a: "LabelSet", b: "LabelSet", seed: int = 0) -> "LabelSet":
+    """Both label sets as one, samples shuffled (so that a later split keeps
+    both kinds on each side)."""
+    adj2 = np.concatenate([a.adj2, b.adj2])
+    shift = len(a.adj2) // 2
+    ns = np.concatenate([a.ns, b.ns])
+    offs = np.concatenate([a.offs, b.offs + shift])
+    roots = np.concatenate([a.roots, b.roots])
+    td = np.concatenate([a.td, b.td])
+    perm = np.random.default_rng(seed).permutation(len(ns))
+    return LabelSet(adj2, ns[perm], offs[perm], roots[perm], td[perm])
+
+
 def label_set(handle: _lib.Handle, graphs: Sequence[Graph], per_graph: int, seed: int = 0,
               min_size: int = 5) -> LabelSet:
     """Every graph (n <= 24) and `per_graph` random connected induced
