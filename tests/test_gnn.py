@@ -120,6 +120,24 @@ def test_label_set_matches_oracle(handle, port):
 
 
 @pytest.mark.gpu
+def test_family_label_set_matches_oracle(handle, port):
+    """The larger in-family labels (gnn.family_label_set): every relabelled
+    subgraph is connected, and its treedepth and optimal-root mask are the
+    oracle's."""
+    graphs = gnn.family_graphs(8, seed=5, n_min=14, n_max=18)
+    data = gnn.family_label_set(handle, graphs, per_graph=6, seed=4, drop=6)
+    assert len(data) == 8 * 7
+    for i in range(len(data)):
+        g = data.graph(i)
+        assert g.is_connected()
+        T = port.dp_table(g)
+        full = (1 << g.n) - 1
+        td = int(T[full])
+        assert data.td[i] == td
+        assert int(data.roots[i]) == sum(1 << v for v in range(g.n) if int(T[full & ~(1 << v)]) == td - 1)
+
+
+@pytest.mark.gpu
 def test_training_on_dp_labels_learns_roots(handle):
     base = G.config3_graphs(count=60, seed=21)
     samples = gnn.label_set(handle, base, per_graph=20, seed=1)
