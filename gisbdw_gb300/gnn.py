@@ -556,12 +556,21 @@ def root_accuracy(net: GNN, data: LabelSet) -> dict:
             "td_mae": float(np.concatenate(err).mean()) if err else None, "samples": len(data)}
 
 
-def guidance(net: GNN, graphs: Sequence[Graph]) -> dict:
+# Levels the hint sits above the rounded td estimate. Decisions above td
+# succeed in a few nodes with the learned order, while those below it are
+# refutations; a window that starts one level up finds the tree of td first
+# and spends less on refutations below td - 1 that the proof of td - 1 makes
+# unnecessary (measured: config 5, 554 proven and a median over all graphs of
+# 19.0 s with offset 1 against 543 and 32.3 s with 0; config 4, 99 against 96).
+HINT_OFFSET = 1
+
+
+def guidance(net: GNN, graphs: Sequence[Graph], hint_offset: int = HINT_OFFSET) -> dict:
     """What the network gives the branch and bound, per graph: the branching
     order (highest score first), an incumbent (the better of the reference
     heuristic chain and a greedy elimination by score, gtd_heuristic kind 3)
-    and a level hint (the rounded td estimate: the decision level tried
-    first). None of it prunes."""
+    and a level hint (the rounded td estimate plus hint_offset: the decision
+    level tried first). None of it prunes."""
     b = make_batch(graphs)
     logits, td_est = net.forward(b)
     scores = [logits[b.graph_start[k]:b.graph_start[k + 1]] for k in range(len(graphs))]
@@ -570,7 +579,7 @@ def guidance(net: GNN, graphs: Sequence[Graph]) -> dict:
     t0, p0 = net.h.heuristic_batch(graphs, 0)
     t1, p1 = net.h.heuristic_batch(graphs, 3, scores)
     seeds = [(int(t1[k]), p1[k]) if t1[k] < t0[k] else (int(t0[k]), p0[k]) for k in range(len(graphs))]
-    hints = np.clip(np.rint(td_est), 1, None).astype(np.int32)
+    hints = np.clip(np.rint(td_est) + hint_offset, 1, None).astype(np.int32)
     return {"orders": orders, "seeds": seeds, "hints": hints, "td_est": td_est}
 
 
