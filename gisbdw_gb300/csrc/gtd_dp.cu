@@ -579,6 +579,12 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
   __shared__ uint64_t stMaskAll[kTreeWarps][kDpMaxN];
   __shared__ int32_t stOwnerAll[kTreeWarps][kDpMaxN];
   __shared__ int32_t stDepthAll[kTreeWarps][kDpMaxN];
+  // The binomial table in shared memory: every lane ranks a different subset,
+  // which the parameter bank would serve one address at a time.
+  __shared__ Binom sBinom;
+  for (int i = threadIdx.x; i < (kDpMaxHigh + 1) * (kDpMaxHigh + 1); i += blockDim.x)
+    (&sBinom[0][0])[i] = (&p.binom[0][0])[i];
+  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t* sAdj = sAdjAll[warp];
   uint64_t* stMask = stMaskAll[warp];
@@ -593,7 +599,7 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
     for (int v = lane; v < n; v += 32)
       sAdj[v] = p.adj[G.adj_off + v];
     __syncwarp();
-    const TreeCtx ctx{p.binom, p.table + G.table_off, G.lb, G.nh, n};
+    const TreeCtx ctx{sBinom, p.table + G.table_off, G.lb, G.nh, n};
     const uint64_t query = p.query ? p.query : (n == 64 ? ~0ull : ((1ull << n) - 1));
     const uint32_t td = query ? ctx.td_of(query) : 0u;
     if (lane == 0 && p.td_out)
@@ -779,9 +785,13 @@ cudaError_t dp_launch_tree(const DpBatchParams& p, cudaStream_t s) {
 __global__ void __launch_bounds__(32 * kTreeWarps)
     dp_labels_kernel(const __grid_constant__ DpBatchParams p, const uint64_t* subsets, int count, int32_t* td_out,
                      uint64_t* roots_out) {
+  __shared__ Binom sBinom;  // lanes rank different subsets: shared memory, not the parameter bank
+  for (int i = threadIdx.x; i < (kDpMaxHigh + 1) * (kDpMaxHigh + 1); i += blockDim.x)
+    (&sBinom[0][0])[i] = (&p.binom[0][0])[i];
+  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const DpGraph G = p.single;
-  const TreeCtx ctx{p.binom, p.table + G.table_off, G.lb, G.nh, G.n};
+  const TreeCtx ctx{sBinom, p.table + G.table_off, G.lb, G.nh, G.n};
   for (int i = blockIdx.x * kTreeWarps + warp; i < count; i += gridDim.x * kTreeWarps) {
     const uint64_t S = subsets[i];
     if (S == 0) {
