@@ -167,7 +167,9 @@ gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_o
   p.parent_out = d_parent;
   p.order_out = d_order;
 
-  int occ = dp_tile_occupancy(p.lb);
+  if (h->dp_occ[p.lb] <= 0)
+    h->dp_occ[p.lb] = dp_tile_occupancy(p.lb);
+  int occ = h->dp_occ[p.lb];
   if (opts && opts->ctas_per_sm > 0 && opts->ctas_per_sm < occ)
     occ = opts->ctas_per_sm;
   if (occ < 1)

@@ -80,6 +80,9 @@ struct gtd_handle_s {
   // Mixed-size kernel throughput over the one-size kernel's, per largest tile
   // size (0 = unmeasured), from the autotuner.
   float tune_mixed_eff[gtd::kTuneLbMax + 1] = {};
+  // CTAs per SM of the one-size DP kernel per tile size (0 = not asked yet):
+  // a property of the kernel and the device, looked up once per handle.
+  int dp_occ[gtd::kDpMaxTileBits + 1] = {};
 
   gtd_bnb_state* bnb = nullptr;
   void* d_scratch = nullptr;  // general device scratch (labels, GNN batches)
