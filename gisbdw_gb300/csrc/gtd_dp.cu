@@ -557,18 +557,19 @@ struct TreeCtx {
     const uint64_t tile = off + rank_colex(binom, H);
     return table[(tile << lb) | (S & ((1ull << lb) - 1))] >> 1;
   }
-  // First vertex v of the connected set C with td(C - v) = td(C) - 1.
+  // First vertex v of the connected set C with td(C - v) = td(C) - 1, i.e.
+  // the first argmin of td(C - v) (td(C) = 1 + min_v td(C - v) for a
+  // connected C): one round of table reads, no read of td(C) itself.
   __device__ int root(uint64_t C) const {
     if (__popcll(C) == 1)
       return __ffsll(static_cast<long long>(C)) - 1;
     const int lane = threadIdx.x & 31;
-    const uint32_t want = td_of(C) - 1u;
-    bool hit_lo = false, hit_hi = false;
-    if ((C >> lane) & 1ull)
-      hit_lo = td_of(C & ~(1ull << lane)) == want;
-    if (lane + 32 < n && ((C >> (lane + 32)) & 1ull))
-      hit_hi = td_of(C & ~(1ull << (lane + 32))) == want;
-    const uint64_t hits = ballot64(hit_lo, hit_hi);
+    const bool in_lo = (C >> lane) & 1ull;
+    const bool in_hi = lane + 32 < n && ((C >> (lane + 32)) & 1ull);
+    const uint32_t t_lo = in_lo ? td_of(C & ~(1ull << lane)) : 0xFFFFFFFFu;
+    const uint32_t t_hi = in_hi ? td_of(C & ~(1ull << (lane + 32))) : 0xFFFFFFFFu;
+    const uint32_t m = __reduce_min_sync(0xffffffffu, min(t_lo, t_hi));
+    const uint64_t hits = ballot64(in_lo && t_lo == m, in_hi && t_hi == m);
     return hits ? __ffsll(static_cast<long long>(hits)) - 1 : -1;
   }
 };
@@ -579,6 +580,11 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
   __shared__ uint64_t stMaskAll[kTreeWarps][kDpMaxN];
   __shared__ int32_t stOwnerAll[kTreeWarps][kDpMaxN];
   __shared__ int32_t stDepthAll[kTreeWarps][kDpMaxN];
+  __shared__ int32_t sParAll[kTreeWarps][kDpMaxN];     // the canonical tree
+  __shared__ int32_t sDepAll[kTreeWarps][kDpMaxN];     // depth of each vertex in it
+  __shared__ uint32_t sHgtAll[kTreeWarps][kDpMaxN];    // subtree height (in vertices)
+  __shared__ uint32_t sLowAll[kTreeWarps][kDpMaxN];    // 255 - the subtree's lowest vertex
+  __shared__ unsigned long long sKidsAll[kTreeWarps][kDpMaxN];  // children of each vertex
   // The binomial table in shared memory: every lane ranks a different subset,
   // which the parameter bank would serve one address at a time.
   __shared__ Binom sBinom;
@@ -605,82 +611,113 @@ __global__ void __launch_bounds__(32 * kTreeWarps)
     if (lane == 0 && p.td_out)
       p.td_out[G.out_idx] = static_cast<int32_t>(td);
 
-    if (p.parent_out) {
-      // Canonical tree: every component is rooted at ctx.root and its
-      // sub-components hang below that root (dynamic_cpu.hpp:59-81).
-      int32_t* parent = p.parent_out + G.adj_off;
-      int top = 0, height = 0;
-      for (uint64_t rest = query; rest;) {
-        const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
-        rest &= ~c;
-        if (lane == 0) {
-          stMask[top] = c;
-          stOwner[top] = -1;
-          stDepth[top] = 1;
-        }
-        ++top;
+    // Canonical tree of the query set: every component is rooted at
+    // ctx.root and its sub-components hang below that root
+    // (dynamic_cpu.hpp:59-81); kept in shared memory for the order below.
+    int32_t* sPar = sParAll[warp];
+    int32_t* sDep = sDepAll[warp];
+    int top = 0, height = 0;
+    for (uint64_t rest = query; rest;) {
+      const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
+      rest &= ~c;
+      if (lane == 0) {
+        stMask[top] = c;
+        stOwner[top] = -1;
+        stDepth[top] = 1;
       }
+      ++top;
+    }
+    __syncwarp();
+    while (top > 0) {
+      --top;
+      const uint64_t C = stMask[top];
+      const int owner = stOwner[top], depth = stDepth[top];
       __syncwarp();
-      while (top > 0) {
-        --top;
-        const uint64_t C = stMask[top];
-        const int owner = stOwner[top], depth = stDepth[top];
-        __syncwarp();
-        const int r = ctx.root(C);
-        if (r < 0) {
-          if (lane == 0)
-            raise_error(p.error, kDevNoRoot, g);
-          return;
-        }
-        if (lane == 0)
-          parent[r] = owner;
-        height = max(height, depth);
-        for (uint64_t rest = C & ~(1ull << r); rest;) {
-          const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
-          rest &= ~c;
-          if (lane == 0) {
-            stMask[top] = c;
-            stOwner[top] = r;
-            stDepth[top] = depth + 1;
-          }
-          ++top;
-        }
-        __syncwarp();
-      }
-      if (static_cast<uint32_t>(height) != td) {
+      const int r = ctx.root(C);
+      if (r < 0) {
         if (lane == 0)
           raise_error(p.error, kDevNoRoot, g);
         return;
       }
+      if (lane == 0) {
+        sPar[r] = owner;
+        sDep[r] = depth;
+      }
+      height = max(height, depth);
+      for (uint64_t rest = C & ~(1ull << r); rest;) {
+        const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
+        rest &= ~c;
+        if (lane == 0) {
+          stMask[top] = c;
+          stOwner[top] = r;
+          stDepth[top] = depth + 1;
+        }
+        ++top;
+      }
+      __syncwarp();
+    }
+    if (static_cast<uint32_t>(height) != td) {
+      if (lane == 0)
+        raise_error(p.error, kDevNoRoot, g);
+      return;
+    }
+    if (p.parent_out) {
+      int32_t* parent = p.parent_out + G.adj_off;
+      for (int v = lane; v < n; v += 32)
+        if ((query >> v) & 1ull)
+          parent[v] = sPar[v];
     }
 
     if (p.order_out) {
       // GetElimination (dynamic_gpu.hpp:58-63): repeatedly remove the stored
       // root of the remaining set; for a disconnected set that is the root of
-      // its first deepest component (dynamic_gpu.cu:92-103).
-      int32_t* order = p.order_out + G.adj_off;
-      uint64_t R = query;
-      for (int step = 0; R; ++step) {
-        uint64_t best = 0;
-        uint32_t best_td = 0;
-        for (uint64_t rest = R; rest;) {
-          const uint64_t c = warp_component(rest, __ffsll(static_cast<long long>(rest)) - 1, sAdj, n);
-          rest &= ~c;
-          const uint32_t t = ctx.td_of(c);
-          if (best == 0 || t > best_td) {
-            best = c;
-            best_td = t;
+      // its first deepest component, components taken in order of their
+      // lowest vertex (dynamic_gpu.cu:92-103). The components of the
+      // remaining set are subtrees of the canonical tree and a component's
+      // treedepth is its subtree's height, so the order is read off the tree:
+      // the active subtree of greatest height, ties to the lowest vertex,
+      // gives its root and is replaced by its children's subtrees.
+      uint32_t* sHgt = sHgtAll[warp];
+      uint32_t* sLow = sLowAll[warp];
+      unsigned long long* sKids = sKidsAll[warp];
+      for (int v = lane; v < n; v += 32) {
+        sHgt[v] = 0u;  // the tallest child so far
+        sLow[v] = 255u - static_cast<uint32_t>(v);
+        sKids[v] = 0ull;
+      }
+      __syncwarp();
+      for (int d = height; d >= 1; --d) {  // deepest first: children before parents
+        for (int v = lane; v < n; v += 32) {
+          if (((query >> v) & 1ull) && sDep[v] == d) {
+            const uint32_t h = sHgt[v] + 1u;  // own height = tallest child + 1
+            sHgt[v] = h;
+            const int pv = sPar[v];
+            if (pv >= 0) {
+              atomicMax(&sHgt[pv], h);
+              atomicMax(&sLow[pv], sLow[v]);
+              atomicOr(&sKids[pv], 1ull << v);
+            }
           }
         }
-        const int r = ctx.root(best);
-        if (r < 0) {
-          if (lane == 0)
-            raise_error(p.error, kDevNoRoot, g);
-          return;
-        }
+        __syncwarp();
+      }
+      int32_t* order = p.order_out + G.adj_off;
+      uint64_t active = 0;
+      for (int v = lane; v < n; v += 32)
+        if (((query >> v) & 1ull) && sPar[v] < 0)
+          active |= 1ull << v;
+      active = warp_or64(active);
+      for (int step = 0; active; ++step) {
+        // key: height << 8 | 255 - lowest vertex (unique: the subtrees are disjoint)
+        const uint32_t k_lo = ((active >> lane) & 1ull) ? (sHgt[lane] << 8 | sLow[lane]) : 0u;
+        const uint32_t k_hi = (lane + 32 < n && ((active >> (lane + 32)) & 1ull))
+                                  ? (sHgt[lane + 32] << 8 | sLow[lane + 32]) : 0u;
+        const uint32_t m = __reduce_max_sync(0xffffffffu, max(k_lo, k_hi));
+        const uint64_t hit = ballot64(k_lo == m && k_lo != 0u, k_hi == m && k_hi != 0u);
+        const int a = __ffsll(static_cast<long long>(hit)) - 1;
         if (lane == 0)
-          order[step] = r;
-        R &= ~(1ull << r);
+          order[step] = a;
+        active = (active & ~(1ull << a)) | sKids[a];
       }
     }
     __syncwarp();

@@ -235,3 +235,84 @@ def test_warp_tile_decode_matches_serial():
     for nh in range(0, 11):
         for t in range(1 << nh):
             assert serial(nh, t) == warp(nh, t), (nh, t)
+
+
+def _canonical_tree(g, T, S):
+    """The canonical elimination forest of the vertex set S from a DP table
+    (every component rooted at its first v with T[C - v] = T[C] - 1):
+    parent and depth per vertex of S."""
+    adj = g.adjacency_masks()
+
+    def comp(R, v):
+        reach, frontier = 1 << v, 1 << v
+        while frontier:
+            nb = 0
+            for u in range(g.n):
+                if frontier >> u & 1:
+                    nb |= adj[u]
+            nb &= R & ~reach
+            reach |= nb
+            frontier = nb
+        return reach
+
+    parent, depth = {}, {}
+    stack = []
+    rest = S
+    while rest:
+        c = comp(rest, (rest & -rest).bit_length() - 1)
+        rest &= ~c
+        stack.append((c, -1, 1))
+    while stack:
+        C, owner, d = stack.pop()
+        if C & (C - 1) == 0:
+            r = C.bit_length() - 1
+        else:
+            r = min((v for v in range(g.n) if C >> v & 1), key=lambda v: (int(T[C & ~(1 << v)]), v))
+        parent[r], depth[r] = owner, d
+        rest = C & ~(1 << r)
+        while rest:
+            c = comp(rest, (rest & -rest).bit_length() - 1)
+            rest &= ~c
+            stack.append((c, r, d + 1))
+    return parent, depth
+
+
+def _order_from_tree(parent):
+    """GetElimination read off the canonical forest (the DP's tree kernel):
+    repeatedly take the active subtree of greatest height, ties to the one
+    with the lowest vertex, emit its root and activate its children."""
+    kids = {v: [] for v in parent}
+    for v, p in parent.items():
+        if p >= 0:
+            kids[p].append(v)
+
+    def hl(v):
+        hs = [hl(c) for c in kids[v]]
+        return (1 + max((h for h, _ in hs), default=0), min([v] + [m for _, m in hs]))
+
+    info = {v: hl(v) for v in parent}
+    active = [v for v, p in parent.items() if p < 0]
+    order = []
+    while active:
+        a = max(active, key=lambda v: (info[v][0], -info[v][1]))
+        order.append(a)
+        active.remove(a)
+        active += kids[a]
+    return order
+
+
+def test_elimination_order_is_read_off_the_canonical_tree(port):
+    """The GetElimination order (dynamic_gpu.hpp:48-64: the root of the first
+    deepest component of the remaining set, repeatedly) equals the traversal
+    of the canonical tree by subtree height, ties to the lowest vertex — the
+    form the GPU tree kernel computes — on full vertex sets and random
+    subsets, connected or not."""
+    rng = np.random.default_rng(7)
+    gs = [G.gnp(n, p, s) for n in (6, 9, 12) for p in (0.2, 0.4) for s in range(3)]
+    gs += [G.grid(3, 4), G.cycle(9), G.Graph(8, [(0, 1), (2, 3), (3, 4), (6, 7)])]
+    for g in gs:
+        T = port.dp_table(g)
+        full = (1 << g.n) - 1
+        for S in [full] + [int(x) for x in rng.integers(1, full + 1, 6)]:
+            parent, _ = _canonical_tree(g, T, S)
+            assert _order_from_tree(parent) == port.get_elimination(g, T, S), (g.name, S)
