@@ -179,26 +179,27 @@ __device__ __forceinline__ bool adjacent_in(const uint64_t* adj, int n, uint64_t
   return u < n && v < n && ((__ldg(adj + u) >> v) & 1ull);
 }
 
-// Checks one graph's adjacency masks: no self loop, no bit >= n, symmetric.
-__device__ bool adjacency_ok(const uint64_t* adj, int n) {
+// Checks each graph's adjacency masks — no self loop, no bit >= n,
+// symmetric — one warp per graph, lane v checking vertex v (and v + 32).
+__global__ void dp_validate_kernel(const __grid_constant__ DpBatchParams p) {
+  const int lane = threadIdx.x & 31;
+  const int g = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (g >= p.num_graphs)
+    return;  // the whole warp
+  const DpGraph G = p.graphs ? p.graphs[g] : p.single;
+  const uint64_t* adj = p.adj + G.adj_off;
+  const int n = G.n;
   const uint64_t allowed = n >= 64 ? ~0ull : ((1ull << n) - 1);
-  for (int v = 0; v < n; ++v) {
+  bool ok = true;
+  for (int v = lane; v < n && ok; v += 32) {
     const uint64_t a = adj[v];
     if (((a >> v) & 1ull) || (a & ~allowed))
-      return false;
-    for (uint64_t s = a; s; s &= s - 1)
+      ok = false;
+    for (uint64_t s = a; s && ok; s &= s - 1)
       if (!((adj[__ffsll(static_cast<long long>(s)) - 1] >> v) & 1ull))
-        return false;
+        ok = false;
   }
-  return true;
-}
-
-__global__ void dp_validate_kernel(const __grid_constant__ DpBatchParams p) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= p.num_graphs)
-    return;
-  const DpGraph G = p.graphs ? p.graphs[g] : p.single;
-  if (!adjacency_ok(p.adj + G.adj_off, G.n))
+  if (__any_sync(0xffffffffu, !ok) && lane == 0)
     raise_error(p.error, kDevInvalidInput, g);
 }
 
@@ -769,7 +770,7 @@ int dp_tile_occupancy(int lb) {
 }
 
 cudaError_t dp_launch_validate(const DpBatchParams& p, cudaStream_t s) {
-  dp_validate_kernel<<<(p.num_graphs + 127) / 128, 128, 0, s>>>(p);
+  dp_validate_kernel<<<(p.num_graphs + 3) / 4, 128, 0, s>>>(p);  // one warp per graph
   return cudaGetLastError();
 }
 
