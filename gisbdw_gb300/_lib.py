@@ -141,14 +141,16 @@ def _ptr(a: np.ndarray) -> ctypes.c_void_p:
     return a.ctypes.data_as(_vp)
 
 
-FAULT_NONE, FAULT_ALLOC, FAULT_STALL = 0, 1, 2
+FAULT_NONE, FAULT_ALLOC, FAULT_STALL, FAULT_POISON = 0, 1, 2, 3
 
 
 def inject_fault(kind: int, count: int = 1) -> None:
     """gtd_inject_fault (tests of the error paths): FAULT_ALLOC makes the
     count-th device allocation from now fail (GTD_OOM); FAULT_STALL makes the
     next count single-graph DP solves wait on a tile nothing computes
-    (GTD_TIMEOUT); FAULT_NONE clears both."""
+    (GTD_TIMEOUT); FAULT_POISON fills the next count DP solves' tables with
+    0xFF first (results unchanged unless a tile is read before it is
+    visible); FAULT_NONE clears all."""
     st = load().gtd_inject_fault(kind, count)
     if st != 0:
         raise _error(st, "gtd_inject_fault")

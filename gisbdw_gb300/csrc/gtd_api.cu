@@ -66,6 +66,16 @@ gtd_status map_device_error(gtd_handle h, int32_t code, int32_t info) {
 namespace {
 std::atomic<int> g_alloc_faults{0};  // pending: the n-th allocation from now fails (0 = none)
 std::atomic<int> g_stall_faults{0};  // pending: DP launches that skip their first tile
+std::atomic<int> g_poison_faults{0};  // pending: DP solves whose table is filled with 0xFF first
+
+bool take_counted(std::atomic<int>& pending) {
+  int n = pending.load();
+  while (n > 0) {
+    if (pending.compare_exchange_weak(n, n - 1))
+      return true;
+  }
+  return false;
+}
 }  // namespace
 
 bool take_alloc_fault() {
@@ -77,14 +87,9 @@ bool take_alloc_fault() {
   return false;
 }
 
-bool take_stall_fault() {
-  int n = g_stall_faults.load();
-  while (n > 0) {
-    if (g_stall_faults.compare_exchange_weak(n, n - 1))
-      return true;
-  }
-  return false;
-}
+bool take_stall_fault() { return take_counted(g_stall_faults); }
+
+bool take_poison_fault() { return take_counted(g_poison_faults); }
 
 cudaError_t ensure_device(void** ptr, size_t* cap, size_t bytes) {
   if (*cap >= bytes && *ptr)
@@ -179,6 +184,8 @@ gtd_status dp_enqueue(gtd_handle h, const uint64_t* d_adj, int n, const gtd_dp_o
     ctas = p.total_tiles;
 
   GTD_CUDA(h, cudaMemsetAsync(h->d_io, 0, 4 * sizeof(int32_t), h->stream));
+  if (take_poison_fault())  // test injection: every byte must be written before it is read
+    GTD_CUDA(h, cudaMemsetAsync(h->d_table, 0xFF, h->table_cap, h->stream));
   if (take_stall_fault())  // test injection: ticket 0 (the level-0 tile) is never taken
     GTD_CUDA(h, cudaMemsetAsync(h->d_io + kIoTicket, 1, 1, h->stream));
   GTD_CUDA(h, dp_launch_validate(p, h->stream));
@@ -512,12 +519,16 @@ gtd_status gtd_inject_fault(int kind, int count) {
     case GTD_FAULT_NONE:
       g_alloc_faults.store(0);
       g_stall_faults.store(0);
+      g_poison_faults.store(0);
       return GTD_OK;
     case GTD_FAULT_ALLOC:
       g_alloc_faults.store(count);
       return GTD_OK;
     case GTD_FAULT_STALL:
       g_stall_faults.store(count);
+      return GTD_OK;
+    case GTD_FAULT_POISON:
+      g_poison_faults.store(count);
       return GTD_OK;
     default:
       return GTD_INVALID_ARG;

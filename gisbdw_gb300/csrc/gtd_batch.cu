@@ -248,8 +248,11 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   const DpBatchParams& cap = h->bparams;
   const bool same_buffers = cap.table == h->d_table && cap.flags == h->d_flags && cap.tile_map == h->d_tile_map &&
                             cap.level_base == h->d_level_base && cap.graphs == h->d_bgraphs;
+  const bool poison = take_poison_fault();  // test injection (gtd_inject_fault)
   if (use_graph && h->bgraph_valid && h->bgraph_key == key && same_buffers) {
     st.graph_replayed = 1;
+    if (poison)
+      GTD_CUDA(h, cudaMemsetAsync(h->d_table, 0xFF, P.table_bytes, h->stream));
     GTD_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
     GTD_CUDA(h, cudaGraphLaunch(h->bgraph, h->stream));
     GTD_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
@@ -302,6 +305,8 @@ gtd_status batch_enqueue(gtd_handle h, const gtd_graph_desc* descs, int count, c
   bp.td_out = d_td;
   bp.parent_out = d_parent;
   GTD_CUDA(h, dp_launch_fill_tile_map(bp, h->stream));
+  if (poison)
+    GTD_CUDA(h, cudaMemsetAsync(h->d_table, 0xFF, P.table_bytes, h->stream));
 
   if (use_graph) {
     if (h->bgraph) {

@@ -29,7 +29,8 @@
 //    a tile's cross-tile children are the whole tiles H - h one level down,
 //    read as contiguous 2^lb-byte blocks (16-byte vector loads through L2);
 //    the in-tile children are resolved in shared memory, 4 subsets per
-//    32-bit word, words in popcount order of the word index.
+//    32-bit word, words in popcount order of the word index, one unrolled
+//    pass per popcount class (its size and child count compile-time).
 //  * Schedule. One persistent launch; every warp is an independent tile
 //    worker (no CTA barriers in the loop). A warp takes a tile by ticket
 //    (atomicAdd) in level-major order and decodes it with ballots over a
@@ -38,9 +39,9 @@
 //    by a deadline). The warp reduces the cross-tile children with OR / AND /
 //    majority logic on 16-byte loads, keeps that summary as two virtual
 //    children in shared memory, resolves the tile there, stores it and
-//    publishes its flag. A tile only waits on tiles with smaller tickets, and
-//    a ticket is only taken by a running warp, so the smallest unfinished
-//    ticket can always proceed.
+//    publishes its flag with a release store. A tile only waits on tiles
+//    with smaller tickets, and a ticket is only taken by a running warp, so
+//    the smallest unfinished ticket can always proceed.
 //
 // Reconstruction (dp_tree_kernel): one warp, one lane per vertex, rebuilds
 // the reference's tree (first-argmin root per component, dynamic_gpu.cu:84-87,
@@ -103,11 +104,18 @@ __device__ __forceinline__ void acc_add1(Acc& c, uint32_t x) {
 }
 
 // Four subsets with |S| >= 3 (connected <=> >= 2 connected children) and at
-// least one child each: per byte s = OR(td) + AND(td) <= 126, so no carries.
-__device__ __forceinline__ uint32_t resolve4(const Acc& c) {
-  const uint32_t s = ((c.o & 0xFEFEFEFEu) + (c.a & 0xFEFEFEFEu)) >> 1;
-  const uint32_t cn = c.d & 0x01010101u;
-  return ((s & 0xFEFEFEFEu) + (((s | cn) & 0x01010101u) << 1)) | cn;
+// least one child each: per byte s = OR(td) + AND(td) <= 126, so no carries;
+// td = (s >> 1) + ((s & 1) | connected), stored as td << 1 | connected.
+__device__ __forceinline__ uint32_t resolve4(uint32_t o, uint32_t a, uint32_t d) {
+  const uint32_t s = ((o & 0xFEFEFEFEu) + (a & 0xFEFEFEFEu)) >> 1;
+  const uint32_t half = (s & 0xFEFEFEFEu) | (d & 0x01010101u);  // 2 (s >> 1) | connected
+  return half + (((s | d) & 0x01010101u) << 1);
+}
+
+__device__ __forceinline__ bool adjacent_in(const uint64_t* adj, int n, uint64_t s2) {
+  const int u = __ffsll(static_cast<long long>(s2)) - 1;
+  const int v = 63 - __clzll(static_cast<long long>(s2));
+  return u < n && v < n && ((__ldg(adj + u) >> v) & 1ull);
 }
 
 // One subset of size k from its children's OR o, AND a and count flag d;
@@ -124,6 +132,53 @@ __device__ __forceinline__ void fold1(uint32_t& o, uint32_t& a, uint32_t& d, uin
   d |= o & v;
   o |= v;
   a &= v;
+}
+
+__device__ __forceinline__ void fold2(uint32_t& o, uint32_t& a, uint32_t& d, uint32_t x, uint32_t y) {
+  d |= (o & (x | y)) | (x & y);  // majority of (any before, x, y)
+  o |= x | y;
+  a &= x & y;
+}
+
+// The word's four subsets (low bits 00, 01, 10, 11), all of size >= 3, from
+// the summary (o, a, d) of their children outside the word: subset 00 is
+// final first and is folded into 01 and 10, which are then final and are
+// folded into 11.
+__device__ __forceinline__ uint32_t resolve_word(uint32_t o, uint32_t a, uint32_t d) {
+  uint32_t v = resolve4(o, a, d);
+  const uint32_t x = __byte_perm(v, 0u, 0x4004u);  // byte 0 into bytes 1 and 2
+  d |= o & x;
+  o |= x;
+  a &= x | 0xFF0000FFu;
+  v = resolve4(o, a, d);
+  const uint32_t y1 = __byte_perm(v, 0u, 0x1444u), y2 = __byte_perm(v, 0u, 0x2444u);  // bytes 1, 2 into 3
+  d |= (o & (y1 | y2)) | (y1 & y2);
+  o |= y1 | y2;
+  a &= (y1 & y2) | 0x00FFFFFFu;
+  return resolve4(o, a, d);
+}
+
+// The same for a word that may hold subsets of size <= 2 (k = |S| of its
+// subset 00; S0 the subset 00 itself): one byte at a time, connectivity of a
+// pair from the adjacency.
+__device__ __forceinline__ uint32_t resolve_word_small(uint32_t go, uint32_t ga, uint32_t gd, int k,
+                                                       const uint64_t* adj, int n, uint64_t S0) {
+  uint32_t o[4], a[4], d[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    o[q] = (go >> (8 * q)) & 0xFFu;
+    a[q] = (ga >> (8 * q)) & 0xFFu;
+    d[q] = (gd >> (8 * q)) & 0xFFu;
+  }
+  const uint32_t v0 = resolve1(o[0], a[0], d[0], k, k == 2 && adjacent_in(adj, n, S0));
+  fold1(o[1], a[1], d[1], v0);
+  fold1(o[2], a[2], d[2], v0);
+  const uint32_t v1 = resolve1(o[1], a[1], d[1], k + 1, k + 1 == 2 && adjacent_in(adj, n, S0 | 1u));
+  const uint32_t v2 = resolve1(o[2], a[2], d[2], k + 1, k + 1 == 2 && adjacent_in(adj, n, S0 | 2u));
+  fold1(o[3], a[3], d[3], v1);
+  fold1(o[3], a[3], d[3], v2);
+  const uint32_t v3 = resolve1(o[3], a[3], d[3], k + 2, k + 2 == 2 && adjacent_in(adj, n, S0 | 3u));
+  return v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
 }
 
 // A word's summary (o, a, d) of at least one child is reproduced by two
@@ -171,12 +226,6 @@ __device__ __forceinline__ uint32_t rank_colex(const Binom& binom, uint32_t H) {
   for (; H; H &= H - 1)
     r += binom[__ffs(H) - 1][++q];
   return r;
-}
-
-__device__ __forceinline__ bool adjacent_in(const uint64_t* adj, int n, uint64_t s2) {
-  const int u = __ffsll(static_cast<long long>(s2)) - 1;
-  const int v = 63 - __clzll(static_cast<long long>(s2));
-  return u < n && v < n && ((__ldg(adj + u) >> v) & 1ull);
 }
 
 // Checks each graph's adjacency masks — no self loop, no bit >= n,
@@ -235,21 +284,113 @@ __device__ void build_word_order(uint16_t* sOrder, const Binom& binom, int bits)
   }
 }
 
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
+}
+
+__device__ __forceinline__ uint32_t lds_u32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
+}
+
+__device__ __forceinline__ void sts_u32(uint32_t addr, uint32_t v) {
+  asm volatile("st.shared.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+__host__ __device__ constexpr uint32_t cbinom(int n, int k) {
+  if (k < 0 || k > n)
+    return 0u;
+  uint64_t r = 1;
+  for (int i = 1; i <= k; ++i)
+    r = r * static_cast<uint64_t>(n - k + i) / static_cast<uint64_t>(i);
+  return static_cast<uint32_t>(r);
+}
+
+// In-tile phase, popcount class S of the word index and every class above
+// it: each lane resolves whole words of the class (listed in sOrder), whose
+// in-tile children are the S words w - b (b a bit of w) of class S - 1,
+// already final in T (shared address tbase); T and U (u_off bytes further)
+// at w hold the cross-tile children's summary as two virtual children. The
+// class size and the number of children are compile-time, so the child loop
+// is unrolled and child w - b is read at A - 4b, A = tbase + 4w, the bits
+// taken lowest first (r4 & (r4 - 4) drops the lowest).
+template <int LB, int S>
+__device__ __forceinline__ void intile_class(const DpBatchParams& p, const DpGraph& G, uint64_t Hfull, int j,
+                                             uint32_t tbase, uint32_t u_off, const uint16_t* sOrder,
+                                             int order_bits) {
+  constexpr int kWordBits = LB - 2;
+  constexpr uint32_t kCount = cbinom(kWordBits, S);
+  const int lane = threadIdx.x & 31;
+#pragma unroll 1
+  for (uint32_t e = lane; e < kCount; e += 32) {
+    const uint32_t w = sOrder[e];
+    const uint32_t A = tbase + (w << 2);
+    uint32_t o = 0u, a = 0xFFFFFFFFu, d = 0u;
+    if (j > 0) {  // the level-0 tile has no cross-tile children
+      const uint32_t x = lds_u32(A), y = lds_u32(A + u_off);
+      o = x | y;
+      a = x & y;
+      d = a;
+    }
+    uint32_t r4 = w << 2;
+#pragma unroll
+    for (int i = 0; i + 2 <= S; i += 2) {
+      const uint32_t n1 = r4 & (r4 - 4u), n2 = n1 & (n1 - 4u);
+      fold2(o, a, d, lds_u32(A + n1 - r4), lds_u32(A + n2 - n1));
+      r4 = n2;
+    }
+    if constexpr ((S & 1) != 0)
+      fold1(o, a, d, lds_u32(A - r4));
+    uint32_t out;
+    if constexpr (S >= 3) {
+      out = resolve_word(o, a, d);
+    } else {
+      if (j + S >= 3)
+        out = resolve_word(o, a, d);
+      else
+        out = resolve_word_small(o, a, d, j + S, p.adj + G.adj_off, G.n, Hfull | (uint64_t(w) << 2));
+    }
+    sts_u32(A, out);
+  }
+  __syncwarp();
+  if constexpr (S < kWordBits)  // the order table's class sizes (order_bits >= kWordBits)
+    intile_class<LB, S + 1>(p, G, Hfull, j, tbase, u_off, sOrder + p.binom[order_bits][S], order_bits);
+}
+
+constexpr uint32_t kNoPending = 0xFFFFFFFFu;
+
+// Publishes the ready flag p.flags[pending] of the tile this warp stored
+// last. The tile's stores are warp-wide instructions of every lane; the
+// warp barrier orders them before lane 0's store, and that store is a
+// gpu-scope release, which is cumulative: a reader that acquires the flag
+// sees every byte of the tile. (No separate fence: the release is the
+// fence.) The tile loops call this right after tile_work returns, before
+// the next ticket, so the flag is not delayed; keeping the release out of
+// tile_work's body lets the one-size kernel fit in 43 registers, 10 CTAs
+// per SM, against 55 with it inside.
+__device__ __forceinline__ void publish_pending(const DpBatchParams& p, uint32_t& pending) {
+  if (pending == kNoPending)
+    return;
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0)
+    st_release_u32(p.flags + pending, p.epoch);
+  pending = kNoPending;
+}
+
 // One warp resolves local tile tl of graph G (tiles of LB bits): waits for
 // its child tiles, reduces them, resolves the tile in T / U (shared memory,
-// 2^LB / 4 words each), stores it and publishes its flag. sOrder is a word
-// order table of order_bits >= LB - 2 bits. False if a wait gave up.
+// 2^LB / 4 words each) and stores it; `pending` then names its flag for
+// publish_pending. sOrder is a word order table of order_bits >= LB - 2
+// bits. False if a wait gave up.
 template <int LB>
 __device__ __forceinline__ bool tile_work(const DpBatchParams& p, const DpGraph& G, uint32_t tl, uint32_t* T,
                                           uint32_t* U, const uint16_t* sOrder, int order_bits, const Binom& sBinom,
-                                          uint32_t* kids) {
+                                          uint32_t* kids, uint32_t& pending) {
   constexpr int kWords = TileShape<LB>::kWords;
-  constexpr int kWordBits = TileShape<LB>::kWordBits;
   const int lane = threadIdx.x & 31;
-  const Binom& binom = p.binom;
   uint8_t* const table = p.table + G.table_off;
   uint32_t* const flags = p.flags + G.tile_base;
-  const uint64_t* const adj = p.adj + G.adj_off;
 
     int j;
     uint32_t H, off_prev;
@@ -328,69 +469,16 @@ __device__ __forceinline__ bool tile_work(const DpBatchParams& p, const DpGraph&
     }
     __syncwarp();
 
-    // In-tile children: words in popcount order of the word index; inside a
-    // word the subsets with low bits 00, then 01 and 10, then 11.
-    const uint64_t Hfull = static_cast<uint64_t>(H) << LB;
-    uint32_t start = 0;
-#pragma unroll 1
-    for (int s = 0; s <= kWordBits; ++s) {
-      const uint32_t count = binom[kWordBits][s];  // words of this popcount class in a tile of LB bits
-      for (uint32_t e = lane; e < count; e += 32) {
-        const uint32_t w = sOrder[start + e];
-        Acc g;
-        acc_init(g);
-        if (j > 0)  // the level-0 tile has no cross-tile children
-          acc_add2(g, T[w], U[w]);
-        uint32_t r = w;
-        for (; __popc(r) >= 2; r &= r - 1, r &= r - 1) {
-          const uint32_t b1 = r & (0u - r);
-          const uint32_t r2 = r & (r - 1);
-          acc_add2(g, T[w ^ b1], T[w ^ (r2 & (0u - r2))]);
-        }
-        if (r)
-          acc_add1(g, T[w ^ r]);
-        const int k = j + s;
-        if (k >= 3) {
-          // subset 00 (byte 0) is final first; fold it into 01 and 10
-          uint32_t v = resolve4(g);
-          const uint32_t x = __byte_perm(v, 0u, 0x4004u);
-          g.d |= g.o & x;
-          g.o |= x;
-          g.a &= x | 0xFF0000FFu;
-          // 01 and 10 (bytes 1, 2) are final; fold both into 11 (byte 3)
-          v = resolve4(g);
-          const uint32_t y1 = __byte_perm(v, 0u, 0x1444u), y2 = __byte_perm(v, 0u, 0x2444u);
-          g.d |= (g.o & (y1 | y2)) | (y1 & y2);
-          g.o |= y1 | y2;
-          g.a &= (y1 & y2) | 0x00FFFFFFu;
-          T[w] = resolve4(g);
-        } else {
-          // small subsets (|S| <= 2 possible): one byte at a time
-          const uint64_t S0 = Hfull | (uint64_t(w) << 2);
-          const int n = G.n;
-          uint32_t o[4], a[4], d[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            o[q] = (g.o >> (8 * q)) & 0xFFu;
-            a[q] = (g.a >> (8 * q)) & 0xFFu;
-            d[q] = (g.d >> (8 * q)) & 0xFFu;
-          }
-          const uint32_t v0 = resolve1(o[0], a[0], d[0], k, k == 2 && adjacent_in(adj, n, S0));
-          fold1(o[1], a[1], d[1], v0);
-          fold1(o[2], a[2], d[2], v0);
-          const uint32_t v1 = resolve1(o[1], a[1], d[1], k + 1, k + 1 == 2 && adjacent_in(adj, n, S0 | 1u));
-          const uint32_t v2 = resolve1(o[2], a[2], d[2], k + 1, k + 1 == 2 && adjacent_in(adj, n, S0 | 2u));
-          fold1(o[3], a[3], d[3], v1);
-          fold1(o[3], a[3], d[3], v2);
-          const uint32_t v3 = resolve1(o[3], a[3], d[3], k + 2, k + 2 == 2 && adjacent_in(adj, n, S0 | 3u));
-          T[w] = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
-        }
-      }
-      start += binom[order_bits][s];  // the order table's class sizes (order_bits >= kWordBits)
-      __syncwarp();
-    }
+    // In-tile children: words in popcount order of the word index, one
+    // unrolled pass per popcount class; inside a word the subsets with low
+    // bits 00, then 01 and 10, then 11.
+    // U lies u_off bytes after T: 2^LB in the one-size kernel, the largest
+    // tile's 2^lb in the mixed one.
+    const uint32_t u_off =
+        static_cast<uint32_t>(reinterpret_cast<const uint8_t*>(U) - reinterpret_cast<const uint8_t*>(T));
+    intile_class<LB, 0>(p, G, static_cast<uint64_t>(H) << LB, j, smem_u32(T), u_off, sOrder, order_bits);
 
-    // Store the tile, then publish it.
+    // Store the tile; the caller publishes it (publish_pending).
     uint32_t* dst = reinterpret_cast<uint32_t*>(table + (size_t(tl) << LB));
     if constexpr (kWords >= 128) {
       for (int w4 = lane; w4 < kWords / 4; w4 += 32)
@@ -399,10 +487,7 @@ __device__ __forceinline__ bool tile_work(const DpBatchParams& p, const DpGraph&
       for (int w = lane; w < kWords; w += 32)
         dst[w] = T[w];
     }
-    __threadfence();
-    __syncwarp();
-    if (lane == 0)
-      st_release_u32(flags + tl, p.epoch);
+    pending = G.tile_base + tl;
     return true;
 }
 
@@ -447,12 +532,13 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   build_word_order(sOrder, p.binom, Shape::kWordBits);
   __syncthreads();
 
-  uint32_t gi, tl;
-  while (next_tile(p, gi, tl)) {
+  uint32_t gi, tl, pending = kNoPending;
+  while (publish_pending(p, pending), next_tile(p, gi, tl)) {
     const DpGraph G = p.graphs ? p.graphs[gi] : p.single;
-    if (!tile_work<LB>(p, G, tl, T, U, sOrder, Shape::kWordBits, sBinom, kids))
+    if (!tile_work<LB>(p, G, tl, T, U, sOrder, Shape::kWordBits, sBinom, kids, pending))
       break;
   }
+  publish_pending(p, pending);
 }
 
 // Batches whose graphs use different tile sizes (DpGraph::lb, 8 .. p.lb):
@@ -482,8 +568,8 @@ __global__ void __launch_bounds__(32 * kDpWarps)
   build_word_order(sOrder, p.binom, bits);
   __syncthreads();
 
-  uint32_t gi, tl;
-  while (next_tile(p, gi, tl)) {
+  uint32_t gi, tl, pending = kNoPending;
+  while (publish_pending(p, pending), next_tile(p, gi, tl)) {
     const DpGraph G = p.graphs[gi];
     bool ok = false;
     if (G.lb > p.lb) {  // the planner never does this: the tile would not fit
@@ -491,16 +577,17 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       break;
     }
     switch (G.lb) {
-      case 8: ok = tile_work<8>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
-      case 9: ok = tile_work<9>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
-      case 10: ok = tile_work<10>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
-      case 11: ok = tile_work<11>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
-      case 12: ok = tile_work<12>(p, G, tl, T, U, sOrder, bits, sBinom, kids); break;
+      case 8: ok = tile_work<8>(p, G, tl, T, U, sOrder, bits, sBinom, kids, pending); break;
+      case 9: ok = tile_work<9>(p, G, tl, T, U, sOrder, bits, sBinom, kids, pending); break;
+      case 10: ok = tile_work<10>(p, G, tl, T, U, sOrder, bits, sBinom, kids, pending); break;
+      case 11: ok = tile_work<11>(p, G, tl, T, U, sOrder, bits, sBinom, kids, pending); break;
+      case 12: ok = tile_work<12>(p, G, tl, T, U, sOrder, bits, sBinom, kids, pending); break;
       default: raise_error(p.error, kDevInvalidInput, static_cast<int32_t>(gi)); break;
     }
     if (!ok)
       break;
   }
+  publish_pending(p, pending);
 }
 
 // Dynamic shared memory of the mixed kernel for tiles of up to lb bits.

@@ -121,10 +121,12 @@ cudaError_t ensure_field(T** field, size_t* cap_elems, size_t count) {
 }
 
 // Test fault injection (gtd_inject_fault), process-wide: consumes one
-// pending device-allocation failure (true: fail this allocation) or one
-// pending DP stall (true: the launch skips its first tile).
+// pending device-allocation failure (true: fail this allocation), one
+// pending DP stall (true: the launch skips its first tile) or one pending
+// table poisoning (true: fill the DP table with 0xFF before the launch).
 bool take_alloc_fault();
 bool take_stall_fault();
+bool take_poison_fault();
 // Grows the flag array; fresh flags are zeroed and the epoch restarts.
 gtd_status ensure_flags(gtd_handle h, size_t tiles);
 // Next epoch for a direct (non-graph) launch.

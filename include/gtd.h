@@ -68,8 +68,14 @@ gtd_status gtd_abort(gtd_handle h);
  *     gtd_dp_solve_device) never take their first tile, so every tile that
  *     depends on it waits until its bound (gtd_dp_opts.timeout_ns) runs out:
  *     GTD_TIMEOUT, and the handle stays usable;
- *   GTD_FAULT_NONE: clears both. */
-enum { GTD_FAULT_NONE = 0, GTD_FAULT_ALLOC = 1, GTD_FAULT_STALL = 2 };
+ *   GTD_FAULT_POISON, c: the next c subset-DP solves (single graphs and
+ *     batches) first fill their table with 0xFF bytes (treedepth 127, a
+ *     value no solve writes). Every table byte is written before any tile
+ *     reads it, so results are unchanged; a tile read before its
+ *     producer's stores were visible would see the poison and corrupt the
+ *     result (the stress test of the tiles' release/acquire publication);
+ *   GTD_FAULT_NONE: clears all. */
+enum { GTD_FAULT_NONE = 0, GTD_FAULT_ALLOC = 1, GTD_FAULT_STALL = 2, GTD_FAULT_POISON = 3 };
 gtd_status gtd_inject_fault(int kind, int count);
 
 /* Options and statistics of one subset-DP solve. */
