@@ -97,6 +97,13 @@ __device__ __forceinline__ void acc_add2(Acc& c, uint32_t x, uint32_t y) {
   c.a &= x & y;
 }
 
+__device__ __forceinline__ void acc_add3(Acc& c, uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t any = x | y | z;
+  c.d |= (c.o & any) | (x & y) | (x & z) | (y & z);  // at least two of (any before, x, y, z)
+  c.o |= any;
+  c.a &= x & y & z;
+}
+
 __device__ __forceinline__ void acc_add1(Acc& c, uint32_t x) {
   c.d |= c.o & x;
   c.o |= x;
@@ -423,8 +430,9 @@ __device__ __forceinline__ bool tile_work(const DpBatchParams& p, const DpGraph&
       return false;
     __syncwarp();  // kids[] written above, read by every lane below
 
-    // Cross-tile children: j whole tiles, 4 subsets per word, children two
-    // at a time.
+    // Cross-tile children: j whole tiles, 4 subsets per word, children three
+    // at a time from 10-bit tiles up (three 16-byte loads in flight per
+    // lane), else two at a time.
     if constexpr (kWords >= 128) {
 #pragma unroll 1
       for (int c0 = 0; c0 < kWords; c0 += 128) {
@@ -433,7 +441,18 @@ __device__ __forceinline__ bool tile_work(const DpBatchParams& p, const DpGraph&
         for (int q = 0; q < 4; ++q)
           acc_init(g[q]);
         int m = 0;
-        for (; m + 2 <= j; m += 2) {
+        for (; LB >= 10 && m + 3 <= j; m += 3) {  // three loads in flight
+          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m]) << LB)) + (c0 >> 2) + lane);
+          const uint4 b =
+              __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m + 1]) << LB)) + (c0 >> 2) + lane);
+          const uint4 c =
+              __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m + 2]) << LB)) + (c0 >> 2) + lane);
+          acc_add3(g[0], a.x, b.x, c.x);
+          acc_add3(g[1], a.y, b.y, c.y);
+          acc_add3(g[2], a.z, b.z, c.z);
+          acc_add3(g[3], a.w, b.w, c.w);
+        }
+        for (; m + 2 <= j; m += 2) {  // pairs: the remainder, or every child below 10 bits
           const uint32_t c_a = kids[m];
           const uint32_t c_b = kids[m + 1];
           const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
@@ -516,8 +535,7 @@ __device__ __forceinline__ bool next_tile(const DpBatchParams& p, uint32_t& gi, 
 // Every tile of the launch has LB bits (single-graph solves, and batches
 // that use one tile size).
 template <int LB>
-__global__ void __launch_bounds__(32 * kDpWarps)
-    dp_tile_kernel(const __grid_constant__ DpBatchParams p) {
+__device__ __forceinline__ void dp_tile_body(const DpBatchParams& p) {
   using Shape = TileShape<LB>;
   extern __shared__ __align__(16) uint8_t smem[];
   const int warp = threadIdx.x >> 5;
@@ -539,6 +557,32 @@ __global__ void __launch_bounds__(32 * kDpWarps)
       break;
   }
   publish_pending(p, pending);
+}
+
+// Tiles of 10 to 12 bits (three cross-tile loads in flight): the launch
+// bound holds the registers to the CTAs per SM that shared memory allows, 10
+// at 10 and 11 bits, 6 at 12.
+template <int LB>
+constexpr int kDpMinCtas = LB >= 12 ? 6 : 10;
+
+template <int LB>
+__global__ void __launch_bounds__(32 * kDpWarps, kDpMinCtas<LB>)
+    dp_tile_kernel(const __grid_constant__ DpBatchParams p) {
+  dp_tile_body<LB>(p);
+}
+
+// Smaller tiles (pairs of cross-tile loads): registers left to the compiler.
+template <int LB>
+__global__ void __launch_bounds__(32 * kDpWarps) dp_tile_kernel_small(const __grid_constant__ DpBatchParams p) {
+  dp_tile_body<LB>(p);
+}
+
+template <int LB>
+constexpr auto tile_kernel_for() {
+  if constexpr (LB >= 10)
+    return &dp_tile_kernel<LB>;
+  else
+    return &dp_tile_kernel_small<LB>;
 }
 
 // Batches whose graphs use different tile sizes (DpGraph::lb, 8 .. p.lb):
@@ -828,17 +872,17 @@ void dp_fill_binom(DpBatchParams& p) {
 
 template <int LB>
 static cudaError_t launch_tiles(const DpBatchParams& p, int ctas, cudaStream_t s) {
-  dp_tile_kernel<LB><<<ctas, 32 * kDpWarps, TileShape<LB>::kSmem, s>>>(p);
+  tile_kernel_for<LB>()<<<ctas, 32 * kDpWarps, TileShape<LB>::kSmem, s>>>(p);
   return cudaGetLastError();
 }
 
 template <int LB>
 static int occupancy_tiles() {
-  if (cudaFuncSetAttribute(dp_tile_kernel<LB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(tile_kernel_for<LB>(), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(TileShape<LB>::kSmem)) != cudaSuccess)
     return 0;
   int blocks = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, dp_tile_kernel<LB>, 32 * kDpWarps,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, tile_kernel_for<LB>(), 32 * kDpWarps,
                                                 TileShape<LB>::kSmem);
   return blocks;
 }
