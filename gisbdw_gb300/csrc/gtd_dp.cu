@@ -399,115 +399,115 @@ __device__ __forceinline__ bool tile_work(const DpBatchParams& p, const DpGraph&
   uint8_t* const table = p.table + G.table_off;
   uint32_t* const flags = p.flags + G.tile_base;
 
-    int j;
-    uint32_t H, off_prev;
-    decode_tile(sBinom, G.nh, tl, j, H, off_prev);
+  int j;
+  uint32_t H, off_prev;
+  decode_tile(sBinom, G.nh, tl, j, H, off_prev);
 
-    // Lane v (a high vertex, v < nh <= 26) with v in H owns child tile
-    // H - v. Its colex rank keeps the terms C(u, i + 1) of the bits u < v and
-    // shifts the bits u > v down one place, C(u, i): a prefix sum and a
-    // suffix sum over the lanes. The child goes to kids[index of v in H].
-    const bool inH = (H >> lane) & 1u;
-    const uint32_t q = __popc(H & ((1u << lane) - 1u));
-    const uint32_t t1 = inH ? sBinom[lane][q + 1] : 0u, t0 = inH ? sBinom[lane][q] : 0u;
-    uint32_t pre = t1, suf = t0;
+  // Lane v (a high vertex, v < nh <= 26) with v in H owns child tile
+  // H - v. Its colex rank keeps the terms C(u, i + 1) of the bits u < v and
+  // shifts the bits u > v down one place, C(u, i): a prefix sum and a
+  // suffix sum over the lanes. The child goes to kids[index of v in H].
+  const bool inH = (H >> lane) & 1u;
+  const uint32_t q = __popc(H & ((1u << lane) - 1u));
+  const uint32_t t1 = inH ? sBinom[lane][q + 1] : 0u, t0 = inH ? sBinom[lane][q] : 0u;
+  uint32_t pre = t1, suf = t0;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t x = __shfl_up_sync(0xffffffffu, pre, d);
-      const uint32_t y = __shfl_down_sync(0xffffffffu, suf, d);
-      if (lane >= d)
-        pre += x;
-      if (lane + d < 32)
-        suf += y;
-    }
-    bool ok = true;
-    if (inH) {
-      const uint32_t child = off_prev + (pre - t1) + (suf - t0);
-      kids[q] = child;
-      ok = wait_flag(flags + child, p.epoch, p.timeout_ns, p.error);
-    }
-    if (__any_sync(0xffffffffu, !ok))
-      return false;
-    __syncwarp();  // kids[] written above, read by every lane below
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t x = __shfl_up_sync(0xffffffffu, pre, d);
+    const uint32_t y = __shfl_down_sync(0xffffffffu, suf, d);
+    if (lane >= d)
+      pre += x;
+    if (lane + d < 32)
+      suf += y;
+  }
+  bool ok = true;
+  if (inH) {
+    const uint32_t child = off_prev + (pre - t1) + (suf - t0);
+    kids[q] = child;
+    ok = wait_flag(flags + child, p.epoch, p.timeout_ns, p.error);
+  }
+  if (__any_sync(0xffffffffu, !ok))
+    return false;
+  __syncwarp();  // kids[] written above, read by every lane below
 
-    // Cross-tile children: j whole tiles, 4 subsets per word, children three
-    // at a time from 10-bit tiles up (three 16-byte loads in flight per
-    // lane), else two at a time.
-    if constexpr (kWords >= 128) {
+  // Cross-tile children: j whole tiles, 4 subsets per word, children three
+  // at a time from 10-bit tiles up (three 16-byte loads in flight per
+  // lane), else two at a time.
+  if constexpr (kWords >= 128) {
 #pragma unroll 1
-      for (int c0 = 0; c0 < kWords; c0 += 128) {
-        Acc g[4];
+    for (int c0 = 0; c0 < kWords; c0 += 128) {
+      Acc g[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          acc_init(g[q]);
-        int m = 0;
-        for (; LB >= 10 && m + 3 <= j; m += 3) {  // three loads in flight
-          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m]) << LB)) + (c0 >> 2) + lane);
-          const uint4 b =
-              __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m + 1]) << LB)) + (c0 >> 2) + lane);
-          const uint4 c =
-              __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m + 2]) << LB)) + (c0 >> 2) + lane);
-          acc_add3(g[0], a.x, b.x, c.x);
-          acc_add3(g[1], a.y, b.y, c.y);
-          acc_add3(g[2], a.z, b.z, c.z);
-          acc_add3(g[3], a.w, b.w, c.w);
-        }
-        for (; m + 2 <= j; m += 2) {  // pairs: the remainder, or every child below 10 bits
-          const uint32_t c_a = kids[m];
-          const uint32_t c_b = kids[m + 1];
-          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
-          const uint4 b = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_b) << LB)) + (c0 >> 2) + lane);
-          acc_add2(g[0], a.x, b.x);
-          acc_add2(g[1], a.y, b.y);
-          acc_add2(g[2], a.z, b.z);
-          acc_add2(g[3], a.w, b.w);
-        }
-        if (m < j) {
-          const uint32_t c_a = kids[m];
-          const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
-          acc_add1(g[0], a.x);
-          acc_add1(g[1], a.y);
-          acc_add1(g[2], a.z);
-          acc_add1(g[3], a.w);
-        }
-        reinterpret_cast<uint4*>(T + c0)[lane] = make_uint4(g[0].o, g[1].o, g[2].o, g[3].o);
-        reinterpret_cast<uint4*>(U + c0)[lane] =
-            make_uint4(second_child(g[0]), second_child(g[1]), second_child(g[2]), second_child(g[3]));
+      for (int q = 0; q < 4; ++q)
+        acc_init(g[q]);
+      int m = 0;
+      for (; LB >= 10 && m + 3 <= j; m += 3) {  // three loads in flight
+        const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m]) << LB)) + (c0 >> 2) + lane);
+        const uint4 b =
+            __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m + 1]) << LB)) + (c0 >> 2) + lane);
+        const uint4 c =
+            __ldcg(reinterpret_cast<const uint4*>(table + (size_t(kids[m + 2]) << LB)) + (c0 >> 2) + lane);
+        acc_add3(g[0], a.x, b.x, c.x);
+        acc_add3(g[1], a.y, b.y, c.y);
+        acc_add3(g[2], a.z, b.z, c.z);
+        acc_add3(g[3], a.w, b.w, c.w);
       }
-    } else {
-      for (int w = lane; w < kWords; w += 32) {
-        Acc g;
-        acc_init(g);
-        for (int m = 0; m < j; ++m) {
-          const uint32_t c_a = kids[m];
-          acc_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(table + (size_t(c_a) << LB)) + w));
-        }
-        T[w] = g.o;
-        U[w] = second_child(g);
+      for (; m + 2 <= j; m += 2) {  // pairs: the remainder, or every child below 10 bits
+        const uint32_t c_a = kids[m];
+        const uint32_t c_b = kids[m + 1];
+        const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
+        const uint4 b = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_b) << LB)) + (c0 >> 2) + lane);
+        acc_add2(g[0], a.x, b.x);
+        acc_add2(g[1], a.y, b.y);
+        acc_add2(g[2], a.z, b.z);
+        acc_add2(g[3], a.w, b.w);
       }
+      if (m < j) {
+        const uint32_t c_a = kids[m];
+        const uint4 a = __ldcg(reinterpret_cast<const uint4*>(table + (size_t(c_a) << LB)) + (c0 >> 2) + lane);
+        acc_add1(g[0], a.x);
+        acc_add1(g[1], a.y);
+        acc_add1(g[2], a.z);
+        acc_add1(g[3], a.w);
+      }
+      reinterpret_cast<uint4*>(T + c0)[lane] = make_uint4(g[0].o, g[1].o, g[2].o, g[3].o);
+      reinterpret_cast<uint4*>(U + c0)[lane] =
+          make_uint4(second_child(g[0]), second_child(g[1]), second_child(g[2]), second_child(g[3]));
     }
-    __syncwarp();
-
-    // In-tile children: words in popcount order of the word index, one
-    // unrolled pass per popcount class; inside a word the subsets with low
-    // bits 00, then 01 and 10, then 11.
-    // U lies u_off bytes after T: 2^LB in the one-size kernel, the largest
-    // tile's 2^lb in the mixed one.
-    const uint32_t u_off =
-        static_cast<uint32_t>(reinterpret_cast<const uint8_t*>(U) - reinterpret_cast<const uint8_t*>(T));
-    intile_class<LB, 0>(p, G, static_cast<uint64_t>(H) << LB, j, smem_u32(T), u_off, sOrder, order_bits);
-
-    // Store the tile; the caller publishes it (publish_pending).
-    uint32_t* dst = reinterpret_cast<uint32_t*>(table + (size_t(tl) << LB));
-    if constexpr (kWords >= 128) {
-      for (int w4 = lane; w4 < kWords / 4; w4 += 32)
-        reinterpret_cast<uint4*>(dst)[w4] = reinterpret_cast<const uint4*>(T)[w4];
-    } else {
-      for (int w = lane; w < kWords; w += 32)
-        dst[w] = T[w];
+  } else {
+    for (int w = lane; w < kWords; w += 32) {
+      Acc g;
+      acc_init(g);
+      for (int m = 0; m < j; ++m) {
+        const uint32_t c_a = kids[m];
+        acc_add1(g, __ldcg(reinterpret_cast<const uint32_t*>(table + (size_t(c_a) << LB)) + w));
+      }
+      T[w] = g.o;
+      U[w] = second_child(g);
     }
-    pending = G.tile_base + tl;
-    return true;
+  }
+  __syncwarp();
+
+  // In-tile children: words in popcount order of the word index, one
+  // unrolled pass per popcount class; inside a word the subsets with low
+  // bits 00, then 01 and 10, then 11.
+  // U lies u_off bytes after T: 2^LB in the one-size kernel, the largest
+  // tile's 2^lb in the mixed one.
+  const uint32_t u_off =
+      static_cast<uint32_t>(reinterpret_cast<const uint8_t*>(U) - reinterpret_cast<const uint8_t*>(T));
+  intile_class<LB, 0>(p, G, static_cast<uint64_t>(H) << LB, j, smem_u32(T), u_off, sOrder, order_bits);
+
+  // Store the tile; the caller publishes it (publish_pending).
+  uint32_t* dst = reinterpret_cast<uint32_t*>(table + (size_t(tl) << LB));
+  if constexpr (kWords >= 128) {
+    for (int w4 = lane; w4 < kWords / 4; w4 += 32)
+      reinterpret_cast<uint4*>(dst)[w4] = reinterpret_cast<const uint4*>(T)[w4];
+  } else {
+    for (int w = lane; w < kWords; w += 32)
+      dst[w] = T[w];
+  }
+  pending = G.tile_base + tl;
+  return true;
 }
 
 // Takes the next ticket (lane 0) and maps it to (graph, local tile);
@@ -588,7 +588,7 @@ constexpr auto tile_kernel_for() {
 // Batches whose graphs use different tile sizes (DpGraph::lb, 8 .. p.lb):
 // shared memory is laid out for the largest (p.lb, a runtime value, so the
 // launch's occupancy follows it) and each tile dispatches on its graph's lb.
-// The five inlined tile sizes raise the register count (62 against 48 for
+// The five inlined tile sizes raise the register count (64 against 47 for
 // one size), so this kernel holds fewer CTAs than the one-size kernel; the
 // autotuner measures that cost and the planner only mixes sizes when the
 // per-size gains outweigh it.

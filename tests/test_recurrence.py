@@ -5,9 +5,10 @@
   td(S) = (s >> 1) + ((s & 1) | connected(S)); a third accumulator tracks
   "at least two connected children". Restated here at the kernel's word
   level (4 subsets per 32-bit word, byte = td << 1 | connected): the
-  cross-tile summary kept as two virtual children, the in-word order
-  00 -> 01, 10 -> 11 with byte permutes, the byte-at-a-time path for
-  |S| <= 2 and the level-0 tile. Checked against the oracle's tables
+  cross-tile summary kept as two virtual children (children reduced two
+  or three at a time), the in-tile children addressed as the unrolled
+  classes address them, the in-word order 00 -> 01, 10 -> 11 with byte
+  permutes, the byte-at-a-time path for |S| <= 2 and the level-0 tile. Checked against the oracle's tables
   (DynamicCPU's values, dynamic_cpu.hpp / dynamic_gpu.cu:68-111).
 * The colex rank of H - v from per-bit terms (prefix and suffix sums), and
   the warp-parallel tile decode (level by running totals, unranking one
@@ -42,11 +43,40 @@ class Acc:
         self.o |= x
         self.a &= x
 
+    def add3(self, x, y, z):
+        any_ = x | y | z
+        self.d |= (self.o & any_) | (x & y) | (x & z) | (y & z)
+        self.o |= any_
+        self.a &= x & y & z
+
 
 def resolve4(g):
+    """The kernel's form: half = 2 (s >> 1) | connected, plus (s & 1 | connected) << 1."""
+    s = ((g.o & 0xFEFEFEFE) + (g.a & 0xFEFEFEFE)) >> 1
+    half = (s & 0xFEFEFEFE) | (g.d & 0x01010101)
+    return (half + (((s | g.d) & 0x01010101) << 1)) & M32
+
+
+def resolve4_reference_form(g):
     s = ((g.o & 0xFEFEFEFE) + (g.a & 0xFEFEFEFE)) >> 1
     cn = g.d & 0x01010101
     return (((s & 0xFEFEFEFE) + (((s | cn) & 0x01010101) << 1)) | cn) & M32
+
+
+def child_words(w, tbase=0x4A0):
+    """In-tile children of word w as the kernel addresses them: A = T + 4w,
+    bits taken lowest first with r4 & (r4 - 4), child at A + n1 - r4 (pairs),
+    then A - r4 for an odd last one; returned as word indices."""
+    A = tbase + 4 * w
+    r4, out = w << 2, []
+    for _ in range(bin(w).count("1") // 2):
+        n1 = r4 & (r4 - 4)
+        n2 = n1 & (n1 - 4)
+        out += [(A + n1 - r4 - tbase) >> 2, (A + n2 - n1 - tbase) >> 2]
+        r4 = n2
+    if bin(w).count("1") & 1:
+        out.append((A - r4 - tbase) >> 2)
+    return out
 
 
 def resolve1(o, a, d, k, adjacent):
@@ -61,9 +91,10 @@ def second_child(g):
     return (g.a & 0xFEFEFEFE) | (g.d & 0x01010101)
 
 
-def word_dp(g, lb):
-    """The kernel's schedule on one graph with tiles of 2^lb subsets; returns
-    the table indexed by subset mask (byte = td << 1 | connected)."""
+def word_dp(g, lb, triples=False):
+    """The kernel's schedule on one graph with tiles of 2^lb subsets (cross-
+    tile children three at a time with `triples`, as from 10-bit tiles up);
+    returns the table indexed by subset mask (byte = td << 1 | connected)."""
     n = g.n
     adj = g.adjacency_masks()
     nh = n - lb
@@ -80,21 +111,28 @@ def word_dp(g, lb):
         T, U = [0] * words, [0] * words
         for w in range(words):
             acc = Acc()
-            for m in range(0, len(kids) - 1, 2):
+            m = 0
+            while triples and m + 3 <= len(kids):
+                acc.add3(word_of(kids[m], w), word_of(kids[m + 1], w), word_of(kids[m + 2], w))
+                m += 3
+            while m + 2 <= len(kids):
                 acc.add2(word_of(kids[m], w), word_of(kids[m + 1], w))
-            if len(kids) % 2:
-                acc.add1(word_of(kids[-1], w))
+                m += 2
+            if m < len(kids):
+                acc.add1(word_of(kids[m], w))
             T[w], U[w] = acc.o, second_child(acc)
         for s in range(lb - 1):
             for w in (x for x in range(words) if bin(x).count("1") == s):
                 acc = Acc()
                 if j > 0:
                     acc.add2(T[w], U[w])
-                for b in range(lb - 2):
-                    if w >> b & 1:
-                        acc.add1(T[w ^ (1 << b)])
+                cw = child_words(w)
+                for i in range(0, len(cw) - 1, 2):
+                    acc.add2(T[cw[i]], T[cw[i + 1]])
+                if len(cw) & 1:
+                    acc.add1(T[cw[-1]])
                 k = j + s
-                if j > 0 and k >= 3:
+                if k >= 3:
                     v = resolve4(acc)
                     x = byte_perm(v, 0, 0x4004)
                     acc.d |= acc.o & x
@@ -160,13 +198,32 @@ GRAPHS = [G.gnp_connected(9, 0.3, 1), G.gnp_connected(10, 0.5, 2), G.sparse_conn
           G.Graph(8, [], name="empty8")]
 
 
-@pytest.mark.parametrize("lb", [4, 6])
-def test_word_level_recurrence_matches_oracle(port, lb):
+@pytest.mark.parametrize("lb,triples", [(4, False), (6, False), (6, True)])
+def test_word_level_recurrence_matches_oracle(port, lb, triples):
     for g in GRAPHS:
-        tab = word_dp(g, lb)
+        tab = word_dp(g, lb, triples)
         assert np.array_equal(tab >> 1, port.dp_table(g)), (g.name, lb)
         conn = connected_flags(g)
         assert np.array_equal(tab[1:] & 1, conn[1:]), (g.name, lb)
+
+
+def test_in_tile_child_addresses():
+    """Every word of a 12-bit tile (10 word bits): the kernel's address steps
+    visit exactly the words w - b, b a bit of w, lowest bit first."""
+    for w in range(1 << 10):
+        assert child_words(w) == [w ^ (1 << b) for b in range(10) if w >> b & 1], w
+
+
+def test_resolve4_forms_agree():
+    """The kernel's resolve4 equals the longer reference form on every word
+    whose bytes hold treedepths < 64 (per-byte sums below 256: no carries)."""
+    rng = np.random.default_rng(5)
+    for _ in range(20000):
+        acc = Acc()
+        acc.o, acc.a, acc.d = (int(x) for x in rng.integers(0, 1 << 32, 3, dtype=np.uint64))
+        acc.o &= 0x7F7F7F7F | 0x01010101
+        acc.a &= 0x7F7F7F7F | 0x01010101
+        assert resolve4(acc) == resolve4_reference_form(acc)
 
 
 def test_two_virtual_children_reproduce_the_summary():
