@@ -791,14 +791,14 @@ struct Search {
           break;
         }
         const int csize = popc128(f.lo, f.hi);
-        int verdict = -1;  // 0 reject, 1 accept
+        int decision = -1;  // 0 reject, 1 accept
         int vroot = -1;
         if (!f.single) {
           if (csize <= fk) {
-            verdict = 1;
+            decision = 1;
             vroot = first128(f.lo, f.hi);
           } else if (fk <= 0 || csize <= 2) {
-            verdict = 0;
+            decision = 0;
           } else {
             MemoHit hit{0, kUnknownUb, 0};
             if (lane == 0)
@@ -807,16 +807,16 @@ struct Search {
             hit.ub = __shfl_sync(0xffffffffu, hit.ub, 0);
             hit.root = __shfl_sync(0xffffffffu, hit.root, 0);
             if (hit.ub <= fk) {
-              verdict = 1;
+              decision = 1;
               vroot = hit.root;
             } else if (hit.lb > fk) {
-              verdict = 0;
+              decision = 0;
             } else if (mini && csize >= kMiniMin && csize <= kMiniMax) {
               int r = 0;
               const int td = mini_dp(f.lo, f.hi, csize, &r);
               if (lane == 0)
                 memo_put(memo, memo_mask, f.lo, f.hi, td, td, r);
-              verdict = td <= fk ? 1 : 0;
+              decision = td <= fk ? 1 : 0;
               vroot = r;
             } else {
               const int ecount = edges(f.lo, f.hi);
@@ -850,9 +850,9 @@ struct Search {
                 }
               }
               if (lb > fk) {
-                verdict = 0;
+                decision = 0;
               } else if (ubr != 0xFFFFFFFFu && static_cast<int>(ubr >> 8) <= fk - 1) {
-                verdict = 1;
+                decision = 1;
                 vroot = static_cast<int>(ubr & 0xFF);
                 if (lane == 0)
                   memo_put(memo, memo_mask, f.lo, f.hi, 0, fk, vroot);
@@ -860,8 +860,8 @@ struct Search {
             }
           }
         }
-        if (verdict >= 0) {
-          ret = verdict == 1;
+        if (decision >= 0) {
+          ret = decision == 1;
           ret_root = vroot;
           --depth;
           continue;
